@@ -1,0 +1,265 @@
+"""TEST INFRASTRUCTURE ONLY: ctypes front end of the CPU oracle (liboracle.so).
+
+Loaded by tests/, the smoke check and bench.py's CPU-baseline leg, and by
+nothing in the product package.  Two restatements of afft's power-of-two FFT
+path live behind it (see afft_oracle.h for file:line citations):
+
+* ``c2c64`` / ``r2c64`` / ``c2r64`` -- the FP64 oracle of the reference test
+  harness (testing.cpp:870-1002), radix-2 Stockham with directly computed
+  twiddles; the numerical ground truth.
+* ``Port32`` -- a scalar FP32 port of afft's own algorithm (radix-4 passes,
+  recurrence twiddles, real pre/post pass), the CPU baseline ("port").
+
+Also ``ref_lib()``: the reference library itself, when oracle/_ref was built
+here from the reference's sources (x86-64 only); used to pin the oracle and to
+generate the golden fixtures.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libafft_ref.so")
+
+C, CI, R, RI = 0, 1, 2, 3
+KINDS = {"c": C, "ci": CI, "r": R, "ri": RI}
+
+_lib = None
+
+
+def build():
+    """Compile liboracle.so with make (gcc only, seconds)."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        P = ctypes.c_void_p
+        I64 = ctypes.c_int64
+        L.oracle_mt19937_uniform.argtypes = [ctypes.c_uint32, I64, ctypes.c_float, ctypes.c_float, P]
+        L.oracle_mt19937_uniform.restype = None
+        L.oracle_mt19937_raw.argtypes = [ctypes.c_uint32, I64, P]
+        L.oracle_mt19937_raw.restype = None
+        for name in ("oracle64_c2c",):
+            getattr(L, name).argtypes = [ctypes.c_int, P, ctypes.c_int, P, P, P, P]
+        L.oracle64_r2c.argtypes = [ctypes.c_int, P, P, P, P]
+        L.oracle64_c2r.argtypes = [ctypes.c_int, P, P, P, P]
+        L.port32_plan_create.argtypes = [ctypes.c_int, ctypes.c_int, P]
+        L.port32_plan_create.restype = P
+        L.port32_plan_destroy.argtypes = [P]
+        L.port32_plan_in_elems.argtypes = [P]
+        L.port32_plan_in_elems.restype = I64
+        L.port32_plan_out_elems.argtypes = [P]
+        L.port32_plan_out_elems.restype = I64
+        L.port32_execute.argtypes = [P, P, P, P, P]
+        L.port32_execute_batch.argtypes = [P, I64, ctypes.c_int, P, P, P, P]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _dims(dims):
+    return np.ascontiguousarray(np.array(dims, dtype=np.int64))
+
+
+def squeeze(dims):
+    """common.hpp:68-84: drop size-1 dims (keep one if all are 1)."""
+    d = [int(x) for x in dims if int(x) != 1]
+    return d or [1]
+
+
+def half_elems(dims):
+    """Elements per array of a real transform's half spectrum: dim 0 halved."""
+    d = squeeze(dims)
+    return (d[0] // 2 + 1) * int(np.prod(d[1:], dtype=np.int64))
+
+
+def mt19937_uniform(count, seed=5489, lo=-1.0, hi=1.0):
+    """The reference harness input generator (testing.cpp:1064-1067);
+    std::mt19937's default seed is 5489."""
+    out = np.empty(count, np.float32)
+    lib().oracle_mt19937_uniform(seed, count, lo, hi, _p(out))
+    return out
+
+
+def mt19937_raw(count, seed=5489):
+    out = np.empty(count, np.uint32)
+    lib().oracle_mt19937_raw(seed, count, _p(out))
+    return out
+
+
+def c2c64(dims, re, im, inverse=False):
+    re = np.ascontiguousarray(re, np.float64).ravel()
+    im = np.ascontiguousarray(im, np.float64).ravel()
+    ore = np.empty_like(re)
+    oim = np.empty_like(im)
+    d = _dims(dims)
+    rc = lib().oracle64_c2c(len(d), _p(d), int(inverse), _p(re), _p(im), _p(ore), _p(oim))
+    if rc:
+        raise ValueError("invalid shape %r" % (dims,))
+    return ore, oim
+
+
+def r2c64(dims, x):
+    x = np.ascontiguousarray(x, np.float64).ravel()
+    h = half_elems(dims)
+    ore = np.empty(h)
+    oim = np.empty(h)
+    d = _dims(dims)
+    if lib().oracle64_r2c(len(d), _p(d), _p(x), _p(ore), _p(oim)):
+        raise ValueError("invalid shape %r" % (dims,))
+    return ore, oim
+
+
+def c2r64(dims, re, im):
+    re = np.ascontiguousarray(re, np.float64).ravel()
+    im = np.ascontiguousarray(im, np.float64).ravel()
+    out = np.empty(int(np.prod(dims, dtype=np.int64)))
+    d = _dims(dims)
+    if lib().oracle64_c2r(len(d), _p(d), _p(re), _p(im), _p(out)):
+        raise ValueError("invalid shape %r" % (dims,))
+    return out
+
+
+def oracle64(kind, dims, a, b=None):
+    """Dispatch by afft kind name ('c', 'ci', 'r', 'ri'); returns float64
+    arrays: (re, im) for c/ci/r, the real array for ri."""
+    if kind == "c":
+        return c2c64(dims, a, b, False)
+    if kind == "ci":
+        return c2c64(dims, a, b, True)
+    if kind == "r":
+        return r2c64(dims, a)
+    if kind == "ri":
+        return c2r64(dims, a, b)
+    raise ValueError(kind)
+
+
+class Port32:
+    """FP32 port of afft (CPU baseline).  Dense batches of one shape."""
+
+    def __init__(self, kind, dims):
+        self.kind = kind
+        self.dims = list(dims)
+        d = _dims(dims)
+        self._h = lib().port32_plan_create(KINDS[kind], len(d), _p(d))
+        if not self._h:
+            raise ValueError("invalid shape %r" % (dims,))
+        self.in_elems = lib().port32_plan_in_elems(self._h)
+        self.out_elems = lib().port32_plan_out_elems(self._h)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().port32_plan_destroy(h)
+            self._h = None
+
+    def __call__(self, a, b=None, batch=1, threads=1, out=None):
+        a = np.ascontiguousarray(a, np.float32).ravel()
+        b = None if b is None else np.ascontiguousarray(b, np.float32).ravel()
+        if out is None:
+            ore = np.empty(batch * self.out_elems, np.float32)
+            oim = None if self.kind == "ri" else np.empty(batch * self.out_elems, np.float32)
+        else:
+            ore, oim = out
+        rc = lib().port32_execute_batch(self._h, batch, threads, _p(a), _p(b), _p(ore), _p(oim))
+        if rc:
+            raise RuntimeError("port32 failed")
+        return ore if self.kind == "ri" else (ore, oim)
+
+
+_ref = None
+
+
+def ref_available():
+    return os.path.exists(REF_PATH)
+
+
+def ref_lib():
+    """The reference afft library built from its own sources (x86-64 here)."""
+    global _ref
+    if _ref is None:
+        L = ctypes.CDLL(REF_PATH)
+        P = ctypes.c_void_p
+        S = ctypes.c_size_t
+        for k in ("c", "ci", "r", "ri"):
+            ms = getattr(L, "afft_32_%s_memsize" % k)
+            ms.restype = S
+            ms.argtypes = [S, P, ctypes.c_int, ctypes.c_int]
+            cr = getattr(L, "afft_32_%s_create" % k)
+            cr.restype = P
+            cr.argtypes = [S, P, ctypes.c_int, P, ctypes.c_int]
+            getattr(L, "afft_32_%s_transform" % k).restype = None
+        L.afft_32_c_transform.argtypes = [P, P, P, P, P]
+        L.afft_32_ci_transform.argtypes = [P, P, P, P, P]
+        L.afft_32_r_transform.argtypes = [P, P, P, P]
+        L.afft_32_ri_transform.argtypes = [P, P, P, P]
+        L.afft_supported.argtypes = [ctypes.c_int]
+        _ref = L
+    return _ref
+
+
+def ref_run(kind, dims, a, b=None, impl=0):
+    """One transform through the reference library's own C API (fft.h)."""
+    L = ref_lib()
+    d = np.array(dims, dtype=np.uint64)
+    ms = getattr(L, "afft_32_%s_memsize" % kind)(len(d), _p(d), 0, impl)
+    if ms == 0:
+        raise ValueError("reference rejected %r impl=%d" % (dims, impl))
+    mem = np.zeros(ms + 64, np.uint8)
+    st = getattr(L, "afft_32_%s_create" % kind)(len(d), _p(d), 0, _p(mem), impl)
+    n = int(np.prod(dims, dtype=np.int64))
+    h = half_elems(dims)
+    a = np.ascontiguousarray(a, np.float32).ravel()
+    b = None if b is None else np.ascontiguousarray(b, np.float32).ravel()
+    if kind in ("c", "ci"):
+        ore = np.zeros(n, np.float32)
+        oim = np.zeros(n, np.float32)
+        getattr(L, "afft_32_%s_transform" % kind)(ctypes.c_void_p(st), _p(a), _p(b), _p(ore), _p(oim))
+        return ore, oim
+    if kind == "r":
+        ore = np.zeros(h, np.float32)
+        oim = np.zeros(h, np.float32)
+        L.afft_32_r_transform(ctypes.c_void_p(st), _p(a), _p(ore), _p(oim))
+        return ore, oim
+    out = np.zeros(n, np.float32)
+    L.afft_32_ri_transform(ctypes.c_void_p(st), _p(a), _p(b), _p(out))
+    return out
+
+
+def rel_l2(y, ref):
+    """Standard relative L2 error ||y - ref|| / ||ref|| over all arrays."""
+    ys = y if isinstance(y, (tuple, list)) else (y,)
+    rs = ref if isinstance(ref, (tuple, list)) else (ref,)
+    num = sum(float(np.sum((np.asarray(a, np.float64) - np.asarray(b, np.float64)) ** 2)) for a, b in zip(ys, rs))
+    den = sum(float(np.sum(np.asarray(b, np.float64) ** 2)) for b in rs)
+    return (num / den) ** 0.5 if den > 0 else num ** 0.5
+
+
+def max_rel(y, ref):
+    """max |y - ref| / max |ref| over all arrays."""
+    ys = y if isinstance(y, (tuple, list)) else (y,)
+    rs = ref if isinstance(ref, (tuple, list)) else (ref,)
+    num = max(float(np.max(np.abs(np.asarray(a, np.float64) - np.asarray(b, np.float64)))) for a, b in zip(ys, rs))
+    den = max(float(np.max(np.abs(np.asarray(b, np.float64)))) for b in rs)
+    return num / den if den > 0 else num
+
+
+def afft_error(y, ref):
+    """The reference harness metric (testing.cpp:1113-1129):
+    sqrt(sum (y-ref)^2 / sum (y^2 + ref^2))."""
+    ys = y if isinstance(y, (tuple, list)) else (y,)
+    rs = ref if isinstance(ref, (tuple, list)) else (ref,)
+    num = sum(float(np.sum((np.asarray(a, np.float64) - np.asarray(b, np.float64)) ** 2)) for a, b in zip(ys, rs))
+    den = sum(float(np.sum(np.asarray(a, np.float64) ** 2 + np.asarray(b, np.float64) ** 2)) for a, b in zip(ys, rs))
+    return (num / den) ** 0.5 if den > 0 else num ** 0.5

@@ -1,0 +1,106 @@
+"""Generate the golden fixtures that pin the oracle and the GPU library to the
+reference afft library's own float outputs.
+
+Runs HERE only (x86-64 with the reference sources): it builds
+oracle/_ref/libafft_ref.so from the reference's source files (oracle/Makefile
+target ``ref``), then for every case calls the reference's C API (fft.h) with
+afft_scalar and with afft_auto (its best SIMD backend on this host) and saves
+inputs and both outputs to ``afft_golden.npz``.  The committed .npz travels to
+the GPU machine; the reference does not.
+
+Inputs follow the reference harness (testing.cpp:1064-1067): std::mt19937
+seeded per case, uniform_real_distribution<float>(-1, 1).  Real-inverse inputs
+are a random (non-Hermitian) half spectrum, so the fixture pins the exact map
+afft computes, including how it ignores the imaginary parts of planes 0 and
+d0/2.  Case 'c1' is the reference harness's own n=1024 input (default seed,
+re block then im block).
+
+    python tests/golden/make_golden.py
+"""
+import json
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle as O  # noqa: E402
+
+AFFT_SCALAR = 1
+AFFT_AUTO = 0
+
+SHAPES = [
+    [1], [2], [4], [8], [16], [32], [64], [128], [256], [512], [1024], [2048],
+    [4096], [8192],
+    [2, 2], [4, 8], [8, 4], [16, 16], [2, 64], [64, 2], [32, 128], [128, 32],
+    [2, 4, 8], [8, 8, 8], [4, 16, 2], [16, 16, 16],
+    [4, 4, 4, 4], [2, 8, 2, 8], [2, 2, 4, 2, 8],
+    [1, 64], [16, 1, 8], [32, 1], [1, 1, 1], [1, 1, 4, 1],
+]
+KINDS = ["c", "ci", "r", "ri"]
+
+
+def cases():
+    seed = 1
+    for dims in SHAPES:
+        n = int(np.prod(dims))
+        for kind in KINDS:
+            # the reference crashes on real transforms of total size 1
+            if kind in ("r", "ri") and n == 1:
+                continue
+            seed += 1
+            yield "%s_%s" % (kind, "x".join(map(str, dims))), kind, dims, seed
+
+
+def main():
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "all", "ref"], check=True)
+    arrays = {}
+    index = []
+    for name, kind, dims, seed in cases():
+        n = int(np.prod(dims))
+        h = O.half_elems(dims)
+        if kind in ("c", "ci"):
+            v = O.mt19937_uniform(2 * n, seed)
+            a, b = v[:n], v[n:]
+        elif kind == "r":
+            a, b = O.mt19937_uniform(n, seed), None
+        else:
+            v = O.mt19937_uniform(2 * h, seed)
+            a, b = v[:h], v[h:]
+        arrays[name + "/in0"] = a
+        if b is not None:
+            arrays[name + "/in1"] = b
+        for tag, impl in (("scalar", AFFT_SCALAR), ("auto", AFFT_AUTO)):
+            out = O.ref_run(kind, dims, a, b, impl)
+            if kind == "ri":
+                arrays[name + "/%s0" % tag] = out
+            else:
+                arrays[name + "/%s0" % tag] = out[0]
+                arrays[name + "/%s1" % tag] = out[1]
+        index.append({"name": name, "kind": kind, "dims": dims, "seed": seed})
+
+    # C1: the reference harness's own n=1024 complex input, then its inverse
+    n = 1024
+    v = O.mt19937_uniform(2 * n, 5489)
+    arrays["c1/in0"], arrays["c1/in1"] = v[:n], v[n:]
+    for tag, impl in (("scalar", AFFT_SCALAR), ("auto", AFFT_AUTO)):
+        fr, fi = O.ref_run("c", [n], v[:n], v[n:], impl)
+        arrays["c1/%s0" % tag], arrays["c1/%s1" % tag] = fr, fi
+        br, bi = O.ref_run("ci", [n], fr, fi, impl)
+        arrays["c1/%s_inv0" % tag], arrays["c1/%s_inv1" % tag] = br / n, bi / n
+    index.append({"name": "c1", "kind": "c", "dims": [n], "seed": 5489})
+
+    np.savez_compressed(os.path.join(HERE, "afft_golden.npz"), **arrays)
+    with open(os.path.join(HERE, "afft_golden.json"), "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py",
+                   "reference_impls": {"scalar": AFFT_SCALAR, "auto": AFFT_AUTO},
+                   "cases": index}, f, indent=1)
+    print("wrote %d cases" % len(index))
+
+
+if __name__ == "__main__":
+    main()
