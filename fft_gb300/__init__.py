@@ -1,0 +1,316 @@
+"""afft_gb300: GB300 power-of-two FFTs behind afft's C API.
+
+The product is ``libafft_gb300.so`` (CUDA kernels + C ABI, see
+include/afft_gb300.h).  This module is its Python front end: ctypes bindings
+of every exported entry point, and classes that mirror afft's C++ wrapper
+fft.hpp (``complex_transform``, ``inverse_complex_transform``,
+``real_transform``, ``inverse_real_transform``; fft.hpp:48-234) with the same
+construction arguments and call signatures, plus ``BatchPlan`` and ``Queue``
+for the batched and multi-transform extensions.
+
+Arrays may be torch CUDA tensors (device pointers: the transform runs on
+device memory) or numpy arrays / CPU tensors (host pointers: the library
+stages the data through device buffers).  There is no CPU fallback: if the
+library cannot be loaded, importing this module raises.
+"""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libafft_gb300.so")
+
+# fft.h:5-15 and the extension enums of include/afft_gb300.h
+afft_auto, afft_scalar, afft_sse2, afft_avx2, afft_avx512f, afft_neon, afft_gb300 = range(7)
+afft_split, afft_interleaved = 0, 1
+KIND_C, KIND_CI, KIND_R, KIND_RI = 0, 1, 2, 3
+KINDS = {"c": KIND_C, "ci": KIND_CI, "r": KIND_R, "ri": KIND_RI}
+ERRORS = {0: "OK", 1: "EINVAL", 2: "ENODEV", 3: "ENOMEM", 4: "ECUDA", 5: "ESTATE", 6: "ETIMEOUT"}
+
+_lib = None
+
+
+class AfftError(RuntimeError):
+    pass
+
+
+class Desc(ctypes.Structure):
+    """afft_gb300_desc"""
+    _fields_ = [("kind", ctypes.c_int), ("ndim", ctypes.c_int), ("dim", ctypes.c_size_t * 3),
+                ("src_re", ctypes.c_void_p), ("src_im", ctypes.c_void_p),
+                ("dst_re", ctypes.c_void_p), ("dst_im", ctypes.c_void_p)]
+
+
+def lib():
+    """The loaded CUDA library.  Raises if it was not built (no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libafft_gb300.so is not built; run `python -m fft_gb300.build`")
+        L = ctypes.CDLL(LIB_PATH)
+        S, P, I = ctypes.c_size_t, ctypes.c_void_p, ctypes.c_int
+        for k in ("c", "ci", "r", "ri"):
+            for bits in ("32", "64"):
+                ms = getattr(L, "afft_%s_%s_memsize" % (bits, k))
+                ms.restype = S
+                ms.argtypes = [S, P, I, I]
+                cr = getattr(L, "afft_%s_%s_create" % (bits, k))
+                cr.restype = P
+                cr.argtypes = [S, P, I, P, I]
+                tr = getattr(L, "afft_%s_%s_transform" % (bits, k))
+                tr.restype = None
+                tr.argtypes = [P, P, P, P, P] if k in ("c", "ci") else [P, P, P, P]
+        L.afft_32_align_size.restype = S
+        L.afft_32_align_size.argtypes = [S]
+        L.afft_64_align_size.restype = S
+        L.afft_64_align_size.argtypes = [S]
+        L.afft_supported.restype = I
+        L.afft_supported.argtypes = [I]
+        L.afft_gb300_last_error.restype = I
+        L.afft_gb300_last_error_string.restype = ctypes.c_char_p
+        L.afft_gb300_batch_memsize.restype = S
+        L.afft_gb300_batch_memsize.argtypes = [I, S, P, S, I]
+        L.afft_gb300_batch_create.restype = P
+        L.afft_gb300_batch_create.argtypes = [I, S, P, S, I, P]
+        L.afft_gb300_transform_async.restype = I
+        L.afft_gb300_transform_async.argtypes = [P, P, P, P, P, P]
+        L.afft_gb300_release.restype = I
+        L.afft_gb300_release.argtypes = [P]
+        L.afft_gb300_plan_launches.restype = I
+        L.afft_gb300_plan_launches.argtypes = [P]
+        L.afft_gb300_queue_create.restype = P
+        L.afft_gb300_queue_create.argtypes = [P, S]
+        L.afft_gb300_queue_run.restype = I
+        L.afft_gb300_queue_run.argtypes = [P, P]
+        L.afft_gb300_queue_launches.restype = I
+        L.afft_gb300_queue_launches.argtypes = [P]
+        L.afft_gb300_queue_destroy.restype = None
+        L.afft_gb300_queue_destroy.argtypes = [P]
+        _lib = L
+    return _lib
+
+
+def last_error():
+    L = lib()
+    return L.afft_gb300_last_error(), L.afft_gb300_last_error_string().decode()
+
+
+def _check(what):
+    code, msg = last_error()
+    if code:
+        raise AfftError("%s: %s (%s)" % (what, msg, ERRORS.get(code, code)))
+
+
+def alignment():
+    return ctypes.c_size_t.in_dll(lib(), "afft_alignment").value
+
+
+def align_size(n):
+    return lib().afft_32_align_size(n)
+
+
+def supported(impl=afft_auto):
+    return bool(lib().afft_supported(impl))
+
+
+def ptr(a):
+    """Address of a torch tensor, numpy array or int (None -> NULL)."""
+    if a is None:
+        return None
+    if isinstance(a, int):
+        return a
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    if hasattr(a, "ctypes"):
+        return a.ctypes.data
+    raise TypeError(type(a))
+
+
+def _dims(dims):
+    dims = [int(d) for d in dims]
+    return (ctypes.c_size_t * max(1, len(dims)))(*dims), len(dims)
+
+
+def squeeze(dims):
+    d = [int(x) for x in dims if int(x) != 1]
+    return d or [1]
+
+
+def half_elems(dims):
+    """Elements per array of a real transform's half spectrum (dim 0 halved,
+    fft_internal.hpp:215-219 without the alignment padding)."""
+    d = squeeze(dims)
+    n = 1
+    for x in d[1:]:
+        n *= x
+    return (d[0] // 2 + 1) * n
+
+
+class _Plan:
+    """A plan placement-built into caller-owned memory (fft.hpp:8-47)."""
+
+    kind = None
+
+    def __init__(self, dims, mem=None, impl=afft_auto, fmt=afft_split):
+        L = lib()
+        self.dims = [int(d) for d in dims]
+        self.format = fmt
+        arr, n = _dims(self.dims)
+        name = {KIND_C: "c", KIND_CI: "ci", KIND_R: "r", KIND_RI: "ri"}[self.kind]
+        size = getattr(L, "afft_32_%s_memsize" % name)(n, arr, fmt, impl)
+        self._mem = None
+        self.state = None
+        if size == 0 or size == ctypes.c_size_t(-1).value:
+            _check("memsize")
+            raise AfftError("memsize rejected the plan")
+        self._mem = mem if mem is not None else ctypes.create_string_buffer(size)
+        self.state = getattr(L, "afft_32_%s_create" % name)(n, arr, fmt, ctypes.addressof(self._mem), impl)
+        if not self.state:
+            _check("create")
+            raise AfftError("create failed")
+        self._fn = getattr(L, "afft_32_%s_transform" % name)
+
+    def __bool__(self):
+        return bool(self.state)
+
+    def release(self):
+        if self.state:
+            lib().afft_gb300_release(self.state)
+            self.state = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+    @property
+    def launches(self):
+        return lib().afft_gb300_plan_launches(self.state)
+
+
+class complex_transform(_Plan):
+    """fft.hpp:48-95: forward complex transform, split or interleaved."""
+    kind = KIND_C
+
+    def __call__(self, src_re, src_im, dst_re, dst_im):
+        self._fn(self.state, ptr(src_re), ptr(src_im), ptr(dst_re), ptr(dst_im))
+        _check("transform")
+
+
+class inverse_complex_transform(complex_transform):
+    """fft.hpp:97-144: unnormalised inverse complex transform."""
+    kind = KIND_CI
+
+
+class real_transform(_Plan):
+    """fft.hpp:146-189: real forward transform, first dim halved."""
+    kind = KIND_R
+
+    def __call__(self, src, dst_re, dst_im):
+        self._fn(self.state, ptr(src), ptr(dst_re), ptr(dst_im))
+        _check("transform")
+
+
+class inverse_real_transform(_Plan):
+    """fft.hpp:191-234: unnormalised real inverse transform."""
+    kind = KIND_RI
+
+    def __call__(self, src_re, src_im, dst):
+        self._fn(self.state, ptr(src_re), ptr(src_im), ptr(dst))
+        _check("transform")
+
+
+class BatchPlan:
+    """``batch`` dense transforms of one shape and kind (extension).
+
+    ``__call__`` is synchronous (like afft); ``launch`` enqueues on a CUDA
+    stream (device pointers only) and returns immediately.
+    """
+
+    def __init__(self, kind, dims, batch, fmt=afft_split):
+        L = lib()
+        self.kind = KINDS[kind] if isinstance(kind, str) else kind
+        self.dims = [int(d) for d in dims]
+        self.batch = int(batch)
+        self.format = fmt
+        arr, n = _dims(self.dims)
+        size = L.afft_gb300_batch_memsize(self.kind, n, arr, self.batch, fmt)
+        self.state = None
+        if size == 0 or size == ctypes.c_size_t(-1).value:
+            _check("batch_memsize")
+            raise AfftError("batch_memsize rejected the plan")
+        self._mem = ctypes.create_string_buffer(size)
+        self.state = L.afft_gb300_batch_create(self.kind, n, arr, self.batch, fmt, ctypes.addressof(self._mem))
+        if not self.state:
+            _check("batch_create")
+            raise AfftError("batch_create failed")
+        name = {KIND_C: "c", KIND_CI: "ci", KIND_R: "r", KIND_RI: "ri"}[self.kind]
+        self._fn = getattr(L, "afft_32_%s_transform" % name)
+
+    def __call__(self, a, b=None, c=None, d=None):
+        if self.kind in (KIND_C, KIND_CI):
+            self._fn(self.state, ptr(a), ptr(b), ptr(c), ptr(d))
+        else:
+            self._fn(self.state, ptr(a), ptr(b), ptr(c))
+        _check("transform")
+
+    def launch(self, src_re, src_im, dst_re, dst_im, stream=None):
+        """Enqueue without waiting; ``stream`` is a torch.cuda.Stream, a raw
+        cudaStream_t int, or None for the plan's own stream."""
+        s = stream.cuda_stream if hasattr(stream, "cuda_stream") else stream
+        rc = lib().afft_gb300_transform_async(self.state, ptr(src_re), ptr(src_im), ptr(dst_re), ptr(dst_im), s)
+        if rc:
+            _check("transform_async")
+
+    @property
+    def launches(self):
+        return lib().afft_gb300_plan_launches(self.state)
+
+    def release(self):
+        if self.state:
+            lib().afft_gb300_release(self.state)
+            self.state = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
+class Queue:
+    """Many transforms of mixed sizes and kinds run as one unit (extension).
+
+    ``descs``: iterable of (kind, dims, src_re, src_im, dst_re, dst_im) with
+    device arrays.
+    """
+
+    def __init__(self, descs):
+        items = list(descs)
+        arr = (Desc * max(1, len(items)))()
+        for i, (kind, dims, sr, si, dr, di) in enumerate(items):
+            d = arr[i]
+            d.kind = KINDS[kind] if isinstance(kind, str) else kind
+            d.ndim = len(dims)
+            for j, x in enumerate(dims):
+                d.dim[j] = int(x)
+            d.src_re, d.src_im, d.dst_re, d.dst_im = ptr(sr), ptr(si), ptr(dr), ptr(di)
+        self._q = lib().afft_gb300_queue_create(arr, len(items))
+        if not self._q:
+            _check("queue_create")
+            raise AfftError("queue_create failed")
+
+    def run(self, stream=None):
+        s = stream.cuda_stream if hasattr(stream, "cuda_stream") else stream
+        if lib().afft_gb300_queue_run(self._q, s):
+            _check("queue_run")
+
+    @property
+    def launches(self):
+        return lib().afft_gb300_queue_launches(self._q)
+
+    def __del__(self):
+        q = getattr(self, "_q", None)
+        if q:
+            lib().afft_gb300_queue_destroy(q)
+            self._q = None

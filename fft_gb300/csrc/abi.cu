@@ -1,0 +1,396 @@
+// The C ABI: afft's fft.h entry points (fft.h:22-84, fft.cpp:139-308) and
+// the extensions declared in include/afft_gb300.h.
+//
+// afft builds a plan by placement into caller memory and has no destroy call
+// (fft_internal.hpp:114-119, fft.hpp:18-44).  Here the caller's `mem` holds a
+// small header (magic, id); the plan object with its device resources lives
+// in a registry keyed by that address, replaced if a new plan is created at
+// the same address, and freed by afft_gb300_release or at unload.
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <unordered_map>
+
+#include "../../include/afft_gb300.h"
+#include "plan.h"
+
+namespace agb {
+
+static thread_local int g_err = 0;
+static thread_local std::string g_msg;
+
+void set_error(int code, const std::string& msg) {
+  g_err = code;
+  g_msg = msg;
+}
+void clear_error() {
+  g_err = 0;
+  g_msg.clear();
+}
+
+static const uint64_t kMagic = 0x3030334247544641ULL;  // "AFTGB300"
+
+struct Header {
+  uint64_t magic;
+  uint64_t id;
+};
+
+struct Registry {
+  std::mutex mu;
+  std::unordered_map<const void*, std::pair<uint64_t, std::shared_ptr<Plan>>> plans;
+  std::atomic<uint64_t> next{1};
+};
+static Registry& reg() {
+  static Registry* r = new Registry();  // leaked on purpose: no teardown-order hazards
+  return *r;
+}
+
+static std::shared_ptr<Plan> lookup(const void* mem) {
+  if (!mem) {
+    set_error(AFFT_GB300_ESTATE, "null plan");
+    return nullptr;
+  }
+  Header h;
+  std::memcpy(&h, mem, sizeof(h));
+  if (h.magic != kMagic) {
+    set_error(AFFT_GB300_ESTATE, "not a plan of this library");
+    return nullptr;
+  }
+  auto& R = reg();
+  std::lock_guard<std::mutex> g(R.mu);
+  auto it = R.plans.find(mem);
+  if (it == R.plans.end() || it->second.first != h.id) {
+    set_error(AFFT_GB300_ESTATE, "plan released or unknown");
+    return nullptr;
+  }
+  return it->second.second;
+}
+
+static int device_ok() {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return 0;
+  }
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) return 0;
+  return prop.major == 10 && prop.minor == 3;
+}
+
+static const size_t kPlanMem = 128;
+
+// memsize checks shared by all kinds: returns 0 when OK, else the value to
+// return from memsize (0 for an error, (size_t)-1 for an unknown format)
+static size_t check_args(size_t ndim, const size_t* dim, int format, int impl, int* nd, long long* dims) {
+  clear_error();
+  if (impl != afft_auto && impl != afft_gb300) {
+    set_error(AFFT_GB300_EINVAL, "impl selects a CPU backend this library does not have");
+    return 0;
+  }
+  if (format != afft_split && format != afft_interleaved) {
+    set_error(AFFT_GB300_EINVAL, "unknown format");
+    return (size_t)-1;
+  }
+  if (ndim > 64 || (ndim > 0 && !dim)) {
+    set_error(AFFT_GB300_EINVAL, "bad ndim");
+    return 0;
+  }
+  if (validate_shape((int)ndim, dim, nd, dims)) {
+    set_error(AFFT_GB300_EINVAL, "dimensions must be powers of two, at most 2^31 elements");
+    return 0;
+  }
+  if (!device_ok()) {
+    set_error(AFFT_GB300_ENODEV, "no GB300 (sm_103) CUDA device");
+    return 0;
+  }
+  return 1;
+}
+
+static size_t memsize_impl(int kind, size_t ndim, const size_t* dim, size_t batch, int format, int impl) {
+  int nd;
+  long long dims[64];
+  size_t r = check_args(ndim, dim, format, impl, &nd, dims);
+  if (r != 1) return r;
+  if (batch == 0) {
+    set_error(AFFT_GB300_EINVAL, "batch must be positive");
+    return 0;
+  }
+  // build a throwaway plan so unsupported shapes fail here, as afft's
+  // memsize is the call that reports them
+  auto P = build_plan(kind, nd, dims, (long long)batch, format);
+  if (!P) return 0;
+  return kPlanMem;
+}
+
+static void* create_impl(int kind, size_t ndim, const size_t* dim, size_t batch, int format, void* mem,
+                         int impl) {
+  int nd;
+  long long dims[64];
+  size_t r = check_args(ndim, dim, format, impl, &nd, dims);
+  if (r != 1) return nullptr;
+  if (!mem || batch == 0) {
+    set_error(AFFT_GB300_EINVAL, "null mem or zero batch");
+    return nullptr;
+  }
+  auto P = build_plan(kind, nd, dims, (long long)batch, format);
+  if (!P) return nullptr;
+  if (cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    set_error(AFFT_GB300_ECUDA, "stream creation failed");
+    return nullptr;
+  }
+  auto& R = reg();
+  Header h{kMagic, R.next++};
+  std::shared_ptr<Plan> sp(P.release());
+  {
+    std::lock_guard<std::mutex> g(R.mu);
+    R.plans[mem] = std::make_pair(h.id, sp);  // replaces a plan built earlier at mem
+  }
+  std::memcpy(mem, &h, sizeof(h));
+  return mem;
+}
+
+static bool is_device_ptr(const void* p) {
+  if (!p) return true;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// Elements per array of one call: input and output, for each data argument
+static void io_elems(const Plan& P, long long* in_n, long long* out_n) {
+  *in_n = P.in_elems * P.batch;
+  *out_n = P.out_elems * P.batch;
+}
+
+static int transform_sync(void* plan, const float* sr, const float* si, float* dr, float* di) {
+  clear_error();
+  auto P = lookup(plan);
+  if (!P) return AFFT_GB300_ESTATE;
+  std::lock_guard<std::mutex> g(P->mu);
+  cudaSetDevice(P->device);
+  const bool real_in = P->kind == K_R, real_out = P->kind == K_RI;
+  const bool inter = P->format == afft_interleaved;
+  // arguments that carry data for this kind/format
+  bool use_si = !real_in && !inter, use_di = !real_out && !inter;
+  bool dev = is_device_ptr(sr) && is_device_ptr(dr) && (!use_si || is_device_ptr(si)) &&
+             (!use_di || is_device_ptr(di));
+  if (dev) {
+    int rc = P->launch(sr, use_si ? si : nullptr, dr, use_di ? di : nullptr, P->stream);
+    if (rc) return rc;
+    cudaError_t e = cudaStreamSynchronize(P->stream);
+    if (e != cudaSuccess) {
+      set_error(AFFT_GB300_ECUDA, cudaGetErrorString(e));
+      return AFFT_GB300_ECUDA;
+    }
+    return 0;
+  }
+  // host data: stage through plan-owned device buffers
+  long long in_n, out_n;
+  io_elems(*P, &in_n, &out_n);
+  size_t fin = (size_t)in_n * (inter && !real_in ? 2 : 1);   // floats of src_re
+  size_t fout = (size_t)out_n * (inter && !real_out ? 2 : 1);
+  size_t need = (fin + (use_si ? fin : 0) + fout + (use_di ? fout : 0)) * sizeof(float);
+  if (P->stage_bytes < need) {
+    if (P->stage) cudaFree(P->stage);
+    P->stage = nullptr;
+    P->stage_bytes = 0;
+    if (cudaMalloc(&P->stage, need) != cudaSuccess) {
+      cudaGetLastError();
+      set_error(AFFT_GB300_ENOMEM, "staging allocation failed");
+      return AFFT_GB300_ENOMEM;
+    }
+    P->stage_bytes = need;
+  }
+  float* d_sr = P->stage;
+  float* d_si = use_si ? d_sr + fin : nullptr;
+  float* d_dr = d_sr + fin + (use_si ? fin : 0);
+  float* d_di = use_di ? d_dr + fout : nullptr;
+  cudaStream_t st = P->stream;
+  cudaMemcpyAsync(d_sr, sr, fin * sizeof(float), cudaMemcpyDefault, st);
+  if (use_si) cudaMemcpyAsync(d_si, si, fin * sizeof(float), cudaMemcpyDefault, st);
+  int rc = P->launch(d_sr, d_si, d_dr, d_di, st);
+  if (rc) return rc;
+  cudaMemcpyAsync(dr, d_dr, fout * sizeof(float), cudaMemcpyDefault, st);
+  if (use_di) cudaMemcpyAsync(di, d_di, fout * sizeof(float), cudaMemcpyDefault, st);
+  cudaError_t e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    set_error(AFFT_GB300_ECUDA, cudaGetErrorString(e));
+    return AFFT_GB300_ECUDA;
+  }
+  return 0;
+}
+
+}  // namespace agb
+
+using namespace agb;
+
+extern "C" {
+
+// ---- fft.h:22-26 ----------------------------------------------------------
+size_t afft_32_c_memsize(size_t ndim, const size_t* dim, int format, int impl) {
+  return memsize_impl(K_C, ndim, dim, 1, format, impl);
+}
+afft_32_c_type* afft_32_c_create(size_t ndim, const size_t* dim, int format, void* mem, int impl) {
+  return (afft_32_c_type*)create_impl(K_C, ndim, dim, 1, format, mem, impl);
+}
+void afft_32_c_transform(afft_32_c_type* st, const float* sr, const float* si, float* dr, float* di) {
+  transform_sync(st, sr, si, dr, di);
+}
+
+// ---- fft.h:28-32 ----------------------------------------------------------
+size_t afft_32_ci_memsize(size_t ndim, const size_t* dim, int format, int impl) {
+  return memsize_impl(K_CI, ndim, dim, 1, format, impl);
+}
+afft_32_ci_type* afft_32_ci_create(size_t ndim, const size_t* dim, int format, void* mem, int impl) {
+  return (afft_32_ci_type*)create_impl(K_CI, ndim, dim, 1, format, mem, impl);
+}
+void afft_32_ci_transform(afft_32_ci_type* st, const float* sr, const float* si, float* dr, float* di) {
+  transform_sync(st, sr, si, dr, di);
+}
+
+// ---- fft.h:34-38 ----------------------------------------------------------
+size_t afft_32_r_memsize(size_t ndim, const size_t* dim, int format, int impl) {
+  return memsize_impl(K_R, ndim, dim, 1, format, impl);
+}
+afft_32_r_type* afft_32_r_create(size_t ndim, const size_t* dim, int format, void* mem, int impl) {
+  return (afft_32_r_type*)create_impl(K_R, ndim, dim, 1, format, mem, impl);
+}
+void afft_32_r_transform(afft_32_r_type* st, const float* src, float* dr, float* di) {
+  transform_sync(st, src, nullptr, dr, di);
+}
+
+// ---- fft.h:40-44 ----------------------------------------------------------
+size_t afft_32_ri_memsize(size_t ndim, const size_t* dim, int format, int impl) {
+  return memsize_impl(K_RI, ndim, dim, 1, format, impl);
+}
+afft_32_ri_type* afft_32_ri_create(size_t ndim, const size_t* dim, int format, void* mem, int impl) {
+  return (afft_32_ri_type*)create_impl(K_RI, ndim, dim, 1, format, mem, impl);
+}
+void afft_32_ri_transform(afft_32_ri_type* st, const float* sr, const float* si, float* dst) {
+  transform_sync(st, sr, si, dst, nullptr);
+}
+
+// ---- fft.h:46 / common.hpp:173-176 ------------------------------------------
+size_t afft_32_align_size(size_t sz) { return (sz + 15) & ~(size_t)15; }
+
+// ---- fft.h:48-80: FP64 is not implemented here ------------------------------
+size_t afft_64_c_memsize(size_t, const size_t*, int, int) {
+  set_error(AFFT_GB300_EINVAL, "FP64 transforms are not implemented");
+  return 0;
+}
+afft_64_c_type* afft_64_c_create(size_t, const size_t*, int, void*, int) { return nullptr; }
+void afft_64_c_transform(afft_64_c_type*, const double*, const double*, double*, double*) {}
+size_t afft_64_ci_memsize(size_t, const size_t*, int, int) {
+  set_error(AFFT_GB300_EINVAL, "FP64 transforms are not implemented");
+  return 0;
+}
+afft_64_ci_type* afft_64_ci_create(size_t, const size_t*, int, void*, int) { return nullptr; }
+void afft_64_ci_transform(afft_64_ci_type*, const double*, const double*, double*, double*) {}
+size_t afft_64_r_memsize(size_t, const size_t*, int, int) {
+  set_error(AFFT_GB300_EINVAL, "FP64 transforms are not implemented");
+  return 0;
+}
+afft_64_r_type* afft_64_r_create(size_t, const size_t*, int, void*, int) { return nullptr; }
+void afft_64_r_transform(afft_64_r_type*, const double*, double*, double*) {}
+size_t afft_64_ri_memsize(size_t, const size_t*, int, int) {
+  set_error(AFFT_GB300_EINVAL, "FP64 transforms are not implemented");
+  return 0;
+}
+afft_64_ri_type* afft_64_ri_create(size_t, const size_t*, int, void*, int) { return nullptr; }
+void afft_64_ri_transform(afft_64_ri_type*, const double*, const double*, double*) {}
+size_t afft_64_align_size(size_t sz) { return (sz + 7) & ~(size_t)7; }
+
+// ---- fft.h:82-84 ------------------------------------------------------------
+int afft_supported(int impl) {
+  if (impl != afft_auto && impl != afft_gb300) return 0;
+  return device_ok();
+}
+
+const size_t afft_alignment = 64;
+
+// ---- extensions ---------------------------------------------------------------
+int afft_gb300_last_error(void) { return g_err; }
+const char* afft_gb300_last_error_string(void) { return g_msg.c_str(); }
+
+size_t afft_gb300_batch_memsize(int kind, size_t ndim, const size_t* dim, size_t batch, int format) {
+  if (kind < 0 || kind > 3) {
+    set_error(AFFT_GB300_EINVAL, "bad kind");
+    return 0;
+  }
+  return memsize_impl(kind, ndim, dim, batch, format, afft_auto);
+}
+
+void* afft_gb300_batch_create(int kind, size_t ndim, const size_t* dim, size_t batch, int format, void* mem) {
+  if (kind < 0 || kind > 3) {
+    set_error(AFFT_GB300_EINVAL, "bad kind");
+    return nullptr;
+  }
+  return create_impl(kind, ndim, dim, batch, format, mem, afft_auto);
+}
+
+int afft_gb300_transform_async(void* plan, const float* sr, const float* si, float* dr, float* di,
+                               void* stream) {
+  clear_error();
+  auto P = lookup(plan);
+  if (!P) return AFFT_GB300_ESTATE;
+  std::lock_guard<std::mutex> g(P->mu);
+  cudaSetDevice(P->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : P->stream;
+  return P->launch(sr, si, dr, di, st);
+}
+
+int afft_gb300_release(void* plan) {
+  clear_error();
+  if (!lookup(plan)) return AFFT_GB300_ESTATE;
+  auto& R = reg();
+  std::shared_ptr<Plan> victim;
+  {
+    std::lock_guard<std::mutex> g(R.mu);
+    auto it = R.plans.find(plan);
+    if (it != R.plans.end()) {
+      victim = it->second.second;
+      R.plans.erase(it);
+    }
+  }
+  Header h{0, 0};
+  std::memcpy(plan, &h, sizeof(h));
+  return 0;
+}
+
+size_t afft_gb300_plan_describe(int kind, size_t ndim, const size_t* dim, size_t batch, int format,
+                                char* buf, size_t buflen) {
+  clear_error();
+  int nd;
+  long long dims[64];
+  if (kind < 0 || kind > 3 || ndim > 64 || (ndim && !dim) || batch == 0 ||
+      (format != afft_split && format != afft_interleaved) || validate_shape((int)ndim, dim, &nd, dims)) {
+    set_error(AFFT_GB300_EINVAL, "bad arguments");
+    return 0;
+  }
+  auto P = build_plan(kind, nd, dims, (long long)batch, format, true);
+  if (!P) return 0;
+  std::string s = describe_plan(*P);
+  if (buf && buflen) {
+    size_t n = std::min(buflen - 1, s.size());
+    std::memcpy(buf, s.data(), n);
+    buf[n] = 0;
+  }
+  return s.size() + 1;
+}
+
+int afft_gb300_plan_launches(const void* plan) {
+  auto P = lookup(plan);
+  return P ? (int)P->ops.size() : -1;
+}
+
+}  // extern "C"

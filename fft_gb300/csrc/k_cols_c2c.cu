@@ -1,0 +1,39 @@
+// cols-mode complex line FFT instantiations, L = 2^0 .. 2^11, plain and
+// with the transposing store of the four-step first pass
+#include "kernels.h"
+namespace agb {
+bool get_cols_c2c(int logl, bool tstore, LineKernel* out) {
+  if (tstore) {
+    switch (logl) {
+      case 0: *out = make_line_kernel<0, true, LK_C2C, true>(); return true;
+      case 1: *out = make_line_kernel<1, true, LK_C2C, true>(); return true;
+      case 2: *out = make_line_kernel<2, true, LK_C2C, true>(); return true;
+      case 3: *out = make_line_kernel<3, true, LK_C2C, true>(); return true;
+      case 4: *out = make_line_kernel<4, true, LK_C2C, true>(); return true;
+      case 5: *out = make_line_kernel<5, true, LK_C2C, true>(); return true;
+      case 6: *out = make_line_kernel<6, true, LK_C2C, true>(); return true;
+      case 7: *out = make_line_kernel<7, true, LK_C2C, true>(); return true;
+      case 8: *out = make_line_kernel<8, true, LK_C2C, true>(); return true;
+      case 9: *out = make_line_kernel<9, true, LK_C2C, true>(); return true;
+      case 10: *out = make_line_kernel<10, true, LK_C2C, true>(); return true;
+      case 11: *out = make_line_kernel<11, true, LK_C2C, true>(); return true;
+    }
+  } else {
+    switch (logl) {
+      case 0: *out = make_line_kernel<0, true, LK_C2C, false>(); return true;
+      case 1: *out = make_line_kernel<1, true, LK_C2C, false>(); return true;
+      case 2: *out = make_line_kernel<2, true, LK_C2C, false>(); return true;
+      case 3: *out = make_line_kernel<3, true, LK_C2C, false>(); return true;
+      case 4: *out = make_line_kernel<4, true, LK_C2C, false>(); return true;
+      case 5: *out = make_line_kernel<5, true, LK_C2C, false>(); return true;
+      case 6: *out = make_line_kernel<6, true, LK_C2C, false>(); return true;
+      case 7: *out = make_line_kernel<7, true, LK_C2C, false>(); return true;
+      case 8: *out = make_line_kernel<8, true, LK_C2C, false>(); return true;
+      case 9: *out = make_line_kernel<9, true, LK_C2C, false>(); return true;
+      case 10: *out = make_line_kernel<10, true, LK_C2C, false>(); return true;
+      case 11: *out = make_line_kernel<11, true, LK_C2C, false>(); return true;
+    }
+  }
+  return false;
+}
+}  // namespace agb

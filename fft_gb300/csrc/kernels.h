@@ -1,0 +1,57 @@
+// Registry of the line-FFT kernel instantiations (one translation unit per
+// family so they compile in parallel).
+#pragma once
+#include "line_fft.cuh"
+
+namespace agb {
+
+typedef void (*LineKernelFn)(LineParams);
+
+struct LineKernel {
+  LineKernelFn fn;
+  int logl;
+  int cols;            // thread mapping: 1 = across lines, 0 = along a line
+  int kind;            // LK_C2C / LK_R2C / LK_C2R
+  int tstore;          // store with the along-line mapping (four-step pass A)
+  int lines_per_cta;   // C
+  int threads;         // T * C
+  size_t smem;         // bytes of dynamic shared memory
+};
+
+constexpr int ROWS_MAX_LOG = 14;   // rows mode: one CTA up to 16384 points
+constexpr int COLS_MAX_LOG = 11;   // cols mode: one CTA up to 2048 points
+
+// rows: kind in {LK_C2C, LK_R2C, LK_C2R}; cols: tstore only with LK_C2C
+bool get_line_kernel(int logl, bool cols, int kind, bool tstore, LineKernel* out);
+
+// per-family lookups (defined in k_*.cu)
+bool get_rows_c2c(int logl, LineKernel* out);
+bool get_rows_r2c(int logl, LineKernel* out);
+bool get_rows_c2r(int logl, LineKernel* out);
+bool get_cols_c2c(int logl, bool tstore, LineKernel* out);
+bool get_cols_real(int logl, int kind, LineKernel* out);
+
+template <int LOGL, bool COLS>
+constexpr int lines_per_cta() {
+  constexpr int T = Sched<LOGL>::T;
+  if constexpr (COLS) return T <= 32 ? 32 : (T <= 64 ? 16 : 8);
+  else return T >= 256 ? 1 : 256 / T;
+}
+
+template <int LOGL, bool COLS, int KIND, bool TSTORE>
+LineKernel make_line_kernel() {
+  constexpr int C = lines_per_cta<LOGL, COLS>();
+  constexpr int L = 1 << LOGL;
+  LineKernel k;
+  k.fn = &line_fft<LOGL, C, COLS, KIND, TSTORE>;
+  k.logl = LOGL;
+  k.cols = COLS;
+  k.kind = KIND;
+  k.tstore = TSTORE;
+  k.lines_per_cta = C;
+  k.threads = Sched<LOGL>::T * C;
+  k.smem = (size_t)2 * C * L * sizeof(float);
+  return k;
+}
+
+}  // namespace agb

@@ -1,0 +1,465 @@
+// Line-FFT kernels for sm_103a: batched power-of-two FFTs along one axis.
+//
+// A "line" is one 1D transform of length L = 2^LOGL along an axis of an array
+// in HBM.  Line q's element i sits at  off(q) + i*es  with
+//     off(q) = (q >> qshift) * hi + (q & qmask) * lo
+// which covers contiguous batches (rows), strided axes of N-D arrays
+// (columns), the interleaved view of real data and the transposed layouts of
+// the four-step decomposition with one formula.
+//
+// One CTA transforms C lines.  Each thread owns E (= 16, or L when L < 16)
+// complex values of one line in registers, in the canonical Stockham layout
+// v[e] = x[t + T*e] (T = L/E threads per line), so the first stage loads
+// straight from HBM and the last stage stores straight to HBM, coalesced:
+//   rows mode (COLS = false): lines are contiguous; consecutive threads walk
+//                             along a line;
+//   cols mode (COLS = true):  consecutive lines are adjacent in memory;
+//                             consecutive threads walk across lines.
+// Stages are radix-16 (one radix-2/4/8 stage first when log2 L is not a
+// multiple of 4); between stages values go through shared memory with an XOR
+// swizzle chosen so the Stockham scatter and the canonical gather are (almost)
+// bank-conflict free.  Stage twiddles come from a per-length table computed
+// in FP64 on the host and rounded once.
+//
+// This restates the work of afft's onedim.hpp (radix-4/8/16 passes,
+// onedim.hpp:55-507) and multi.hpp (passes along strided dims,
+// multi.hpp:18-259) as one self-sorting (Stockham) formulation, so no
+// bit-reversal pass (onedim.hpp:397-447) is needed; the real pre/post passes
+// (onedim.hpp:1031-1108, multi.hpp:343-414) are fused into the first/last
+// stage; inverse transforms swap re and im on load and store, the identity
+// afft uses for its inverse plans (common.hpp:355-378).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace agb {
+
+enum LineKind { LK_C2C = 0, LK_R2C = 1, LK_C2R = 2 };
+
+struct LineIO {
+  float* re;
+  float* im;
+  long long es;       // element stride (floats)
+  long long lo, hi;   // off(q) = (q >> qshift) * hi + (q & qmask) * lo
+  int qshift;
+  long long qmask;
+};
+
+struct LineParams {
+  LineIO in, out;
+  long long nlines;         // lines to transform
+  const float2* tw;         // stage twiddles for this L
+  // four-step twiddle W_N^{((q >> tw_qshift) & tw_qmask) * k}: N = tw_n
+  // (0 = none),
+  // W_N^m = tw_hi[m >> tw_lo_bits] * tw_lo[m & ((1 << tw_lo_bits) - 1)]
+  const float2* tw_hi;
+  const float2* tw_lo;
+  long long tw_n;
+  long long tw_qmask;
+  int tw_qshift;
+  int tw_lo_bits;
+  const float2* rtw;        // real pass twiddles W_{2L}^k, k < L
+  int inverse;              // swap re/im on load and store
+};
+
+// ---------------------------------------------------------------------------
+// compile-time radix schedule
+// ---------------------------------------------------------------------------
+template <int LOGL>
+struct Sched {
+  static constexpr int L = 1 << LOGL;
+  static constexpr int E = LOGL < 4 ? L : 16;
+  static constexpr int T = L / E;
+  static constexpr int FIRST = (LOGL >= 4 && (LOGL % 4)) ? (1 << (LOGL % 4)) : 0;
+  static constexpr int NSTAGES = LOGL < 4 ? 1 : (LOGL / 4 + (FIRST ? 1 : 0));
+  static constexpr int radix(int s) { return LOGL < 4 ? L : (FIRST && s == 0 ? FIRST : 16); }
+  static constexpr int ns(int s) {
+    int r = 1;
+    for (int i = 0; i < s; i++) r *= radix(i);
+    return r;
+  }
+  static constexpr int twoff(int s) {
+    int o = 0;
+    for (int i = 0; i < s; i++)
+      if (ns(i) > 1) o += (radix(i) - 1) * ns(i);
+    return o;
+  }
+  static constexpr int twsize() { return twoff(NSTAGES); }
+};
+
+// ---------------------------------------------------------------------------
+// complex helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+__device__ __forceinline__ float2 cmul_negi(float2 a) { return make_float2(a.y, -a.x); }   // -i*a
+__device__ __forceinline__ float2 cswap(float2 a) { return make_float2(a.y, a.x); }
+
+// constants: cos/sin(pi/8), sqrt(1/2)
+#define AFFT_C8 0.92387953251128674f
+#define AFFT_S8 0.38268343236508979f
+#define AFFT_R2 0.70710678118654752f
+
+// W16^k * a for k = 1..9 (forward, exp(-2 pi i k/16))
+template <int K>
+__device__ __forceinline__ float2 w16(float2 a) {
+  if constexpr (K == 0) return a;
+  else if constexpr (K == 1) return cmul(a, make_float2(AFFT_C8, -AFFT_S8));
+  else if constexpr (K == 2) return make_float2(AFFT_R2 * (a.x + a.y), AFFT_R2 * (a.y - a.x));
+  else if constexpr (K == 3) return cmul(a, make_float2(AFFT_S8, -AFFT_C8));
+  else if constexpr (K == 4) return cmul_negi(a);
+  else if constexpr (K == 6) return make_float2(AFFT_R2 * (a.y - a.x), -AFFT_R2 * (a.x + a.y));
+  else if constexpr (K == 9) return cmul(a, make_float2(-AFFT_C8, AFFT_S8));
+  else return a;  // unused
+}
+
+__device__ __forceinline__ void dft2(float2& a, float2& b) {
+  float2 t = a;
+  a = cadd(t, b);
+  b = csub(t, b);
+}
+
+// in-place DFT-4 on (a0, a1, a2, a3), natural order out
+__device__ __forceinline__ void dft4(float2& a0, float2& a1, float2& a2, float2& a3) {
+  float2 s02 = cadd(a0, a2), d02 = csub(a0, a2);
+  float2 s13 = cadd(a1, a3), d13 = csub(a1, a3);
+  a0 = cadd(s02, s13);
+  a2 = csub(s02, s13);
+  a1 = cadd(d02, cmul_negi(d13));
+  a3 = csub(d02, cmul_negi(d13));
+}
+
+template <int R>
+__device__ __forceinline__ void dft(float2 (&x)[R]) {
+  if constexpr (R == 1) {
+  } else if constexpr (R == 2) {
+    dft2(x[0], x[1]);
+  } else if constexpr (R == 4) {
+    dft4(x[0], x[1], x[2], x[3]);
+  } else if constexpr (R == 8) {
+    // 2 x 4: E = DFT4(even), O = DFT4(odd) * W8^k
+    dft4(x[0], x[2], x[4], x[6]);
+    dft4(x[1], x[3], x[5], x[7]);
+    x[3] = w16<2>(x[3]);
+    x[5] = w16<4>(x[5]);
+    x[7] = w16<6>(x[7]);
+    float2 y[8];
+    y[0] = cadd(x[0], x[1]); y[4] = csub(x[0], x[1]);
+    y[1] = cadd(x[2], x[3]); y[5] = csub(x[2], x[3]);
+    y[2] = cadd(x[4], x[5]); y[6] = csub(x[4], x[5]);
+    y[3] = cadd(x[6], x[7]); y[7] = csub(x[6], x[7]);
+#pragma unroll
+    for (int i = 0; i < 8; i++) x[i] = y[i];
+  } else if constexpr (R == 16) {
+    // n = n1 + 4 n2, k = k2 + 4 k1
+#pragma unroll
+    for (int n1 = 0; n1 < 4; n1++) dft4(x[n1], x[n1 + 4], x[n1 + 8], x[n1 + 12]);
+    // now x[n1 + 4 k2] = Y[n1][k2]; twiddle W16^{n1 k2}
+    x[5] = w16<1>(x[5]);  x[9] = w16<2>(x[9]);   x[13] = w16<3>(x[13]);
+    x[6] = w16<2>(x[6]);  x[10] = w16<4>(x[10]); x[14] = w16<6>(x[14]);
+    x[7] = w16<3>(x[7]);  x[11] = w16<6>(x[11]); x[15] = w16<9>(x[15]);
+#pragma unroll
+    for (int k2 = 0; k2 < 4; k2++) dft4(x[4 * k2], x[4 * k2 + 1], x[4 * k2 + 2], x[4 * k2 + 3]);
+    // now x[4 k2 + k1] = X[k2 + 4 k1]: transpose the 4x4 index
+    float2 y[16];
+#pragma unroll
+    for (int k2 = 0; k2 < 4; k2++)
+#pragma unroll
+      for (int k1 = 0; k1 < 4; k1++) y[k2 + 4 * k1] = x[4 * k2 + k1];
+#pragma unroll
+    for (int i = 0; i < 16; i++) x[i] = y[i];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// shared-memory layouts (split re/im float arrays)
+// ---------------------------------------------------------------------------
+template <int L, int C, bool COLS>
+struct Smem {
+  float* re;
+  float* im;
+  __device__ __forceinline__ int idx(int c, int j) const {
+    if constexpr (COLS) {
+      constexpr int LC = C >= 32 ? 5 : (C >= 16 ? 4 : (C >= 8 ? 3 : (C >= 4 ? 2 : (C >= 2 ? 1 : 0))));
+      if constexpr (C == 1) return j;
+      else return j * C + (c ^ ((j >> (5 - LC)) & (C - 1)));
+    } else {
+      int f = c * L + j;
+      return f ^ (((f >> 5) & 15) | ((f >> 4) & 16)) ^ ((f >> 9) & 31);
+    }
+  }
+  __device__ __forceinline__ void put(int c, int j, float2 v) const {
+    int k = idx(c, j);
+    re[k] = v.x;
+    im[k] = v.y;
+  }
+  __device__ __forceinline__ float2 get(int c, int j) const {
+    int k = idx(c, j);
+    return make_float2(re[k], im[k]);
+  }
+};
+
+template <bool WARP_ONLY>
+__device__ __forceinline__ void line_sync() {
+  if constexpr (WARP_ONLY) __syncwarp();
+  else __syncthreads();
+}
+
+__device__ __forceinline__ long long line_off(const LineIO& io, long long q) {
+  return (q >> io.qshift) * io.hi + (q & io.qmask) * io.lo;
+}
+
+__device__ __forceinline__ float2 ldg2(const float2* p) { return __ldg(p); }
+
+// One Stockham stage: B = E/R butterflies per thread, butterfly b = t + T*u
+// reads slots u + B*r, applies W_{NS*R}^{r*(b mod NS)}, DFT-R, and either
+// scatters to shared memory (non-last) or keeps the canonical layout (last).
+template <int R, int NS, int E, int T, bool LAST, class SM>
+__device__ __forceinline__ void stage(float2 (&v)[E], int t, int c, const float2* tw, const SM& sm,
+                                      bool do_write) {
+  constexpr int B = E / R;
+#pragma unroll
+  for (int u = 0; u < B; u++) {
+    const int b = t + T * u;
+    float2 x[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) x[r] = v[u + B * r];
+    if constexpr (NS > 1) {
+      const int k = b & (NS - 1);
+#pragma unroll
+      for (int r = 1; r < R; r++) x[r] = cmul(x[r], ldg2(tw + (r - 1) * NS + k));
+    }
+    dft<R>(x);
+    if constexpr (LAST) {
+#pragma unroll
+      for (int r = 0; r < R; r++) v[u + B * r] = x[r];
+    } else {
+      if (do_write) {
+        const int base = (b / NS) * NS * R + (b & (NS - 1));
+#pragma unroll
+        for (int r = 0; r < R; r++) sm.put(c, base + r * NS, x[r]);
+      }
+    }
+  }
+}
+
+// All stages; v holds the input in canonical layout on entry and the output
+// in canonical layout on exit.
+template <int LOGL, int C, bool COLS, bool WARP_ONLY, int S>
+__device__ __forceinline__ void run_stages(float2 (&v)[Sched<LOGL>::E], int t, int c, const float2* tw,
+                                           const Smem<Sched<LOGL>::L, C, COLS>& sm) {
+  using Sc = Sched<LOGL>;
+  constexpr int E = Sc::E, T = Sc::T;
+  if constexpr (S < Sc::NSTAGES) {
+    constexpr int R = Sc::radix(S);
+    constexpr int NS = Sc::ns(S);
+    constexpr bool LAST = S == Sc::NSTAGES - 1;
+    if constexpr (S > 0) {
+      // values of the previous stage are in shared memory
+#pragma unroll
+      for (int e = 0; e < E; e++) v[e] = sm.get(c, t + T * e);
+    }
+    if constexpr (!LAST) {
+      if constexpr (S > 0) line_sync<WARP_ONLY>();   // everyone finished reading
+      stage<R, NS, E, T, false>(v, t, c, tw + Sc::twoff(S), sm, true);
+      line_sync<WARP_ONLY>();                          // writes visible
+      run_stages<LOGL, C, COLS, WARP_ONLY, S + 1>(v, t, c, tw, sm);
+    } else {
+      stage<R, NS, E, T, true>(v, t, c, tw + Sc::twoff(S), sm, false);
+    }
+  }
+}
+
+__device__ __forceinline__ float2 fourstep_twiddle(const LineParams& p, long long q, int k) {
+  long long m = (((q >> p.tw_qshift) & p.tw_qmask) * (long long)k) & (p.tw_n - 1);
+  float2 a = ldg2(p.tw_hi + (m >> p.tw_lo_bits));
+  float2 b = ldg2(p.tw_lo + (m & ((1LL << p.tw_lo_bits) - 1)));
+  return cmul(a, b);
+}
+
+// ---------------------------------------------------------------------------
+// the kernel
+// ---------------------------------------------------------------------------
+template <int LOGL, int C, bool COLS, int KIND, bool TSTORE>
+__global__ void __launch_bounds__(Sched<LOGL>::T * C)
+line_fft(const LineParams p) {
+  using Sc = Sched<LOGL>;
+  constexpr int L = Sc::L, E = Sc::E, T = Sc::T;
+  // a line lives inside one warp: rows mode with T <= 32, or a single line
+  constexpr bool WARP_ONLY = (!COLS && T <= 32) || (T * C <= 32);
+  extern __shared__ float smem_raw[];
+  Smem<L, C, COLS> sm{smem_raw, smem_raw + C * L};
+
+  const int tid = threadIdx.x;
+  const int c = COLS ? (tid % C) : (tid / T);
+  const int t = COLS ? (tid / C) : (tid % T);
+  const long long q = (long long)blockIdx.x * C + c;
+  const bool active = q < p.nlines;
+
+  float2 v[E];
+  if constexpr (KIND == LK_C2R) {
+    // real inverse pre-pass (onedim.hpp:1064-1068 / multi.hpp:366-370 with
+    // inverse): Z'[i] = a - i*b, a = X[i] + conj(X[L-i]),
+    // b = (conj(X[L-i]) - X[i]) * conj(w_i); Z'[0] from the real parts of
+    // X[0] and X[L]; then the inverse transform of Z' (swap trick).
+    if (active) {
+      const long long base = line_off(p.in, q);
+#pragma unroll
+      for (int e = 0; e < E; e++) {
+        const int i = t + T * e;
+        const long long a0 = base + (long long)i * p.in.es;
+        const long long a1 = base + (long long)(L - i) * p.in.es;
+        float2 s0 = make_float2(__ldg(p.in.re + a0), __ldg(p.in.im + a0));
+        float2 s1 = make_float2(__ldg(p.in.re + a1), __ldg(p.in.im + a1));
+        float2 z;
+        if (i == 0) {
+          z = make_float2(s0.x + s1.x, s0.x - s1.x);
+        } else {
+          float2 w = ldg2(p.rtw + i);
+          float2 a = cadd(s0, cconj(s1));
+          float2 b = cmul(csub(cconj(s1), s0), cconj(w));
+          z = cadd(a, cmul_negi(b));
+        }
+        v[e] = cswap(z);
+      }
+    } else {
+#pragma unroll
+      for (int e = 0; e < E; e++) v[e] = make_float2(0.f, 0.f);
+    }
+  } else {
+    if (active) {
+      const long long base = line_off(p.in, q);
+#pragma unroll
+      for (int e = 0; e < E; e++) {
+        const long long a = base + (long long)(t + T * e) * p.in.es;
+        v[e] = make_float2(__ldg(p.in.re + a), __ldg(p.in.im + a));
+      }
+      if (p.inverse) {
+#pragma unroll
+        for (int e = 0; e < E; e++) v[e] = cswap(v[e]);
+      }
+    } else {
+#pragma unroll
+      for (int e = 0; e < E; e++) v[e] = make_float2(0.f, 0.f);
+    }
+  }
+
+  run_stages<LOGL, C, COLS, WARP_ONLY, 0>(v, t, c, p.tw, sm);
+
+  if constexpr (KIND == LK_C2C) {
+    if (p.tw_n) {
+#pragma unroll
+      for (int e = 0; e < E; e++) v[e] = cmul(v[e], fourstep_twiddle(p, q, t + T * e));
+    }
+    if (p.inverse) {
+#pragma unroll
+      for (int e = 0; e < E; e++) v[e] = cswap(v[e]);
+    }
+    if constexpr (TSTORE) {
+      // computed with the cols mapping, stored with the rows mapping
+      if constexpr (Sc::NSTAGES > 1) line_sync<false>();
+#pragma unroll
+      for (int e = 0; e < E; e++) sm.put(c, t + T * e, v[e]);
+      __syncthreads();
+      const int c2 = tid / T, t2 = tid % T;
+      const long long q2 = (long long)blockIdx.x * C + c2;
+      if (q2 < p.nlines) {
+        const long long base = line_off(p.out, q2);
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+          const float2 x = sm.get(c2, t2 + T * e);
+          const long long a = base + (long long)(t2 + T * e) * p.out.es;
+          p.out.re[a] = x.x;
+          p.out.im[a] = x.y;
+        }
+      }
+    } else if (active) {
+      const long long base = line_off(p.out, q);
+#pragma unroll
+      for (int e = 0; e < E; e++) {
+        const long long a = base + (long long)(t + T * e) * p.out.es;
+        p.out.re[a] = v[e].x;
+        p.out.im[a] = v[e].y;
+      }
+    }
+  } else if constexpr (KIND == LK_C2R) {
+    if (active) {
+      const long long base = line_off(p.out, q);
+#pragma unroll
+      for (int e = 0; e < E; e++) {
+        const float2 z = cswap(v[e]);
+        const long long a = base + (long long)(t + T * e) * p.out.es;
+        p.out.re[a] = z.x;
+        p.out.im[a] = z.y;
+      }
+    }
+  } else {
+    // real forward post-pass (onedim.hpp:1058-1108 / multi.hpp:354-414):
+    // X[k] = a - i*b, a = (Z[k] + conj(Z[L-k]))/2,
+    // b = (Z[k] - conj(Z[L-k])) * w_k / 2; X[0], X[L] from Z[0].
+    if constexpr (Sc::NSTAGES > 1) line_sync<WARP_ONLY>();
+#pragma unroll
+    for (int e = 0; e < E; e++) sm.put(c, t + T * e, v[e]);
+    line_sync<WARP_ONLY>();
+    if (active) {
+      const long long base = line_off(p.out, q);
+#pragma unroll
+      for (int e = 0; e < E; e++) {
+        const int k = t + T * e;
+        const float2 s0 = v[e];
+        const float2 s1 = sm.get(c, (L - k) & (L - 1));
+        float2 x;
+        if (k == 0) {
+          x = make_float2(s0.x + s0.y, 0.f);
+          const long long aL = base + (long long)L * p.out.es;
+          p.out.re[aL] = s0.x - s0.y;
+          p.out.im[aL] = 0.f;
+        } else {
+          const float2 w = ldg2(p.rtw + k);
+          const float2 a = make_float2(0.5f * (s0.x + s1.x), 0.5f * (s0.y - s1.y));
+          const float2 d = make_float2(0.5f * (s0.x - s1.x), 0.5f * (s0.y + s1.y));
+          const float2 b = cmul(d, w);
+          x = cadd(a, cmul_negi(b));
+        }
+        const long long a = base + (long long)k * p.out.es;
+        p.out.re[a] = x.x;
+        p.out.im[a] = x.y;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// standalone real pre/post pass for transforms too long for one CTA
+// ---------------------------------------------------------------------------
+struct RealPassParams {
+  LineIO in, out;
+  long long nlines;
+  long long L;            // complex length (real length 2L)
+  const float2* rtw;      // W_{2L}^k, k < L
+  int inverse;            // 0: Z -> X (forward post), 1: X -> Z' (inverse pre)
+  int lines_fastest;      // thread index walks lines first (cols layout)
+};
+
+// Thread (q, k) with k in [0, L/2] handles the pair (k, L-k) of line q, so
+// the pass can run in place.
+__global__ void real_pass_kernel(const RealPassParams p);
+
+// Copies `nlines` lines of `len` complex elements between two layouts (used
+// to pack/unpack the row-pair view of N-D real data around a four-step pass).
+struct CopyParams {
+  LineIO in, out;
+  long long nlines, len;
+};
+__global__ void copy_lines_kernel(const CopyParams p);
+
+// Real transforms of total size 1: X[0] = x[0] + 0i (forward), x[0] = re X[0]
+// (inverse), one element per line.
+__global__ void real1_kernel(const RealPassParams p);
+
+}  // namespace agb

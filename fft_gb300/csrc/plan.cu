@@ -1,0 +1,638 @@
+// Plan construction and execution.
+//
+// Mapping of afft's composition (fft_internal.hpp) onto GPU passes:
+//  - complex N-D (fft_internal.hpp:121-164): one pass per axis, last axis
+//    first; the first pass reads src and writes dst, the others run in place
+//    on dst.  An axis of length <= 2^14 (contiguous) or <= 2^11 (strided) is
+//    one pass; a longer axis takes two passes (four-step: L = L1*L2, a pass
+//    over L1 with the W_L^{t2 k1} twiddle fused into its epilogue, then a pass
+//    over L2), through a plan-owned scratch buffer.
+//  - inverse (fft_internal.hpp:166-198): the same passes with re/im swapped
+//    on load and store.
+//  - real 1D (onedim.hpp:1110-1254): the n/2-point complex transform of the
+//    interleaved view with the real post/pre pass fused into the kernel; for
+//    n/2 > 2^14 the four-step passes plus a standalone real pass.
+//  - real N-D (fft_internal.hpp:200-493): dim 0 is halved; the halved dim-0
+//    pass with the fused real pass, and the complex (N-1)-D transform of each
+//    of the d0/2+1 planes in place on dst (reverse order for the inverse,
+//    through scratch).
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+
+#include "plan.h"
+
+namespace agb {
+
+// ---------------------------------------------------------------------------
+// twiddles: exp(-2 pi i m / N) in FP64 with exact quadrant/octant symmetry,
+// rounded once to FP32
+// ---------------------------------------------------------------------------
+static void unit_root(long long m, long long N, double* c, double* s) {
+  m %= N;
+  if (m < 0) m += N;
+  if (N == 1 || m == 0) { *c = 1.0; *s = 0.0; return; }
+  if (N == 2) { *c = -1.0; *s = 0.0; return; }
+  const double pi = 3.14159265358979323846;
+  double cc, ss;  // cos/sin of +2 pi m / N
+  if (N % 4 == 0) {
+    long long q4 = N / 4;
+    long long quad = m / q4, r = m % q4;
+    double c0, s0;
+    if (N % 8 == 0 && r > N / 8) {
+      long long r2 = q4 - r;  // complementary angle
+      double a = 2.0 * pi * (double)r2 / (double)N;
+      c0 = std::sin(a);
+      s0 = std::cos(a);
+    } else {
+      double a = 2.0 * pi * (double)r / (double)N;
+      c0 = std::cos(a);
+      s0 = std::sin(a);
+    }
+    if (r == 0) { c0 = 1.0; s0 = 0.0; }
+    switch (quad) {
+      case 0: cc = c0; ss = s0; break;
+      case 1: cc = -s0; ss = c0; break;
+      case 2: cc = -c0; ss = -s0; break;
+      default: cc = s0; ss = -c0; break;
+    }
+  } else {
+    double a = 2.0 * pi * (double)m / (double)N;
+    cc = std::cos(a);
+    ss = std::sin(a);
+  }
+  *c = cc;
+  *s = -ss;  // forward sign
+}
+
+static float2 root_f(long long m, long long N) {
+  double c, s;
+  unit_root(m, N, &c, &s);
+  return make_float2((float)c, (float)s);
+}
+
+struct TableCache {
+  std::mutex mu;
+  std::map<std::pair<int, long long>, float2*> tables;  // (device*4 + type, key)
+};
+static TableCache& tcache() {
+  static TableCache* c = new TableCache();  // never destroyed: outlives static plans
+  return *c;
+}
+
+static const float2* upload(int type, long long key, const std::vector<float2>& host) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  auto& C = tcache();
+  std::lock_guard<std::mutex> g(C.mu);
+  auto id = std::make_pair(dev * 4 + type, key);
+  auto it = C.tables.find(id);
+  if (it != C.tables.end()) return it->second;
+  float2* d = nullptr;
+  size_t bytes = std::max<size_t>(host.size(), 1) * sizeof(float2);
+  if (cudaMalloc(&d, bytes) != cudaSuccess) return nullptr;
+  if (!host.empty()) cudaMemcpy(d, host.data(), host.size() * sizeof(float2), cudaMemcpyHostToDevice);
+  C.tables[id] = d;
+  return d;
+}
+
+// Stage twiddles of the line kernel for L = 2^logl: for each stage s with
+// NS = ns(s) > 1 and radix R, entries [(r-1)*NS + k] = W_{NS R}^{r k}.
+template <int LOGL>
+static std::vector<float2> stage_table() {
+  using S = Sched<LOGL>;
+  std::vector<float2> t(S::twsize());
+  for (int s = 0; s < S::NSTAGES; s++) {
+    int ns = S::ns(s), R = S::radix(s);
+    if (ns == 1) continue;
+    int off = S::twoff(s);
+    for (int r = 1; r < R; r++)
+      for (int k = 0; k < ns; k++) t[off + (r - 1) * ns + k] = root_f((long long)r * k, (long long)ns * R);
+  }
+  return t;
+}
+
+template <int... Ls>
+static std::vector<float2> stage_table_dispatch(int logl, std::integer_sequence<int, Ls...>) {
+  std::vector<float2> out;
+  ((logl == Ls ? (void)(out = stage_table<Ls>()) : (void)0), ...);
+  return out;
+}
+
+const float2* stage_twiddles(int logl) {
+  return upload(0, logl, stage_table_dispatch(logl, std::make_integer_sequence<int, 15>{}));
+}
+
+const float2* real_twiddles(long long L) {
+  std::vector<float2> t(L);
+  for (long long k = 0; k < L; k++) t[k] = root_f(k, 2 * L);
+  return upload(1, L, t);
+}
+
+void fourstep_tables(long long N, const float2** hi, const float2** lo, int* lo_bits) {
+  int lb = 0;
+  while ((1LL << (2 * lb)) < N) lb++;  // lo covers about sqrt(N) entries
+  long long nlo = 1LL << lb, nhi = (N + nlo - 1) / nlo;
+  std::vector<float2> th(nhi), tl(nlo);
+  for (long long j = 0; j < nhi; j++) th[j] = root_f(j * nlo, N);
+  for (long long j = 0; j < nlo; j++) tl[j] = root_f(j, N);
+  *hi = upload(2, N, th);
+  *lo = upload(3, N, tl);
+  *lo_bits = lb;
+}
+
+// ---------------------------------------------------------------------------
+// plan building
+// ---------------------------------------------------------------------------
+static int ilog2ll(long long v) {
+  int r = 0;
+  while ((1LL << r) < v) r++;
+  return r;
+}
+
+// A complex array view: element i of re at re.off + i*unit (floats), im
+// likewise.  bstride = complex elements between consecutive outer blocks.
+struct View {
+  Ref re, im;
+  long long unit = 1;
+};
+
+static View split_view(int bre, int bim, long long off = 0) {
+  View v;
+  v.re = {bre, off};
+  v.im = {bim, off};
+  v.unit = 1;
+  return v;
+}
+static View inter_view(int b, long long off = 0) {  // re,im pairs in one array
+  View v;
+  v.re = {b, off};
+  v.im = {b, off + 1};
+  v.unit = 2;
+  return v;
+}
+
+static IOSpec io(const View& v, long long es, long long lo, long long hi, int qshift, long long qmask) {
+  IOSpec s;
+  s.re = v.re;
+  s.im = v.im;
+  s.es = es * v.unit;
+  s.lo = lo * v.unit;
+  s.hi = hi * v.unit;
+  s.qshift = qshift;
+  s.qmask = qmask;
+  return s;
+}
+
+struct Builder {
+  Plan& P;
+  bool ok = true;
+  std::string err;
+  long long scr_base = 0;  // floats of scratch reserved below four-step use
+  bool dry = false;        // describe only: no device tables
+  explicit Builder(Plan& p, bool d = false) : P(p), dry(d) {}
+
+  void fail(const std::string& m) {
+    if (ok) err = m;
+    ok = false;
+  }
+
+  void need_scratch(long long floats) { P.scratch_floats = std::max(P.scratch_floats, floats); }
+
+  void line(int kind, bool cols, bool tstore, int logl, const IOSpec& in, const IOSpec& out,
+            long long nlines, bool inverse, long long tw_n = 0, long long tw_qmask = 0,
+            int tw_qshift = 0, long long real_L = 0) {
+    if (!ok) return;
+    Op op;
+    op.type = OP_LINE;
+    if (!get_line_kernel(logl, cols, kind, tstore, &op.k)) {
+      fail("no kernel for this line length");
+      return;
+    }
+    op.in = in;
+    op.out = out;
+    op.p.nlines = nlines;
+    op.p.inverse = inverse ? 1 : 0;
+    op.real_L = real_L;
+    op.p.tw_n = tw_n;
+    op.p.tw_qmask = tw_qmask;
+    op.p.tw_qshift = tw_qshift;
+    if (!dry) {
+      op.p.tw = stage_twiddles(logl);
+      if (tw_n) fourstep_tables(tw_n, &op.p.tw_hi, &op.p.tw_lo, &op.p.tw_lo_bits);
+      if (real_L) op.p.rtw = real_twiddles(real_L);
+    }
+    op.grid = (nlines + op.k.lines_per_cta - 1) / op.k.lines_per_cta;
+    op.threads = op.k.threads;
+    op.smem = op.k.smem;
+    if (!dry && (!op.p.tw || (tw_n && (!op.p.tw_hi || !op.p.tw_lo)) || (real_L && !op.p.rtw))) {
+      fail("twiddle table allocation failed");
+      return;
+    }
+    P.ops.push_back(op);
+  }
+
+  void real_pass(const IOSpec& in, const IOSpec& out, long long nlines, long long L, bool inverse,
+                 bool lines_fastest) {
+    if (!ok) return;
+    Op op;
+    op.type = OP_REAL;
+    op.in = in;
+    op.out = out;
+    op.rp.nlines = nlines;
+    op.rp.L = L;
+    op.rp.rtw = dry ? nullptr : real_twiddles(L);
+    op.rp.inverse = inverse ? 1 : 0;
+    op.rp.lines_fastest = lines_fastest ? 1 : 0;
+    op.threads = 256;
+    op.grid = (nlines * (L / 2 + 1) + 255) / 256;
+    if (!dry && !op.rp.rtw) fail("twiddle table allocation failed");
+    P.ops.push_back(op);
+  }
+
+  void copy(const IOSpec& in, const IOSpec& out, long long nlines, long long len) {
+    if (!ok) return;
+    Op op;
+    op.type = OP_COPY;
+    op.in = in;
+    op.out = out;
+    op.cp.nlines = nlines;
+    op.cp.len = len;
+    op.threads = 256;
+    op.grid = (nlines * len + 255) / 256;
+    P.ops.push_back(op);
+  }
+
+  void real1(bool forward, long long count) {
+    if (!ok) return;
+    Op op;
+    op.type = OP_REAL1;
+    op.rp.nlines = count;
+    op.rp.inverse = forward ? 0 : 1;
+    View v;
+    if (forward) {
+      op.in = io(split_view(B_SRC_RE, B_SRC_RE), 1, 0, 1, 0, 0);
+      op.out = io(P.format == 1 ? inter_view(B_DST_RE) : split_view(B_DST_RE, B_DST_IM), 1, 0, 1, 0, 0);
+    } else {
+      op.in = io(P.format == 1 ? inter_view(B_SRC_RE) : split_view(B_SRC_RE, B_SRC_IM), 1, 0, 1, 0, 0);
+      op.out = io(split_view(B_DST_RE, B_DST_RE), 1, 0, 1, 0, 0);
+    }
+    (void)v;
+    op.threads = 256;
+    op.grid = (count + 255) / 256;
+    P.ops.push_back(op);
+  }
+
+  // Complex transform along the middle axis of a dense (outer, L, inner)
+  // array, from view A to view B (may be the same).  a_bs / b_bs: complex
+  // elements between outer blocks (default L*inner).
+  void axis(long long outer, long long L, long long inner, const View& A, const View& B,
+            bool inverse, long long a_bs = 0, long long b_bs = 0) {
+    if (!ok) return;
+    if (a_bs == 0) a_bs = L * inner;
+    if (b_bs == 0) b_bs = L * inner;
+    int logl = ilog2ll(L);
+    if (inner == 1) {
+      if (logl <= ROWS_MAX_LOG) {
+        line(LK_C2C, false, false, logl, io(A, 1, 0, a_bs, 0, 0), io(B, 1, 0, b_bs, 0, 0), outer, inverse);
+        return;
+      }
+      // four-step along a contiguous axis
+      int l1 = (logl + 1) / 2, l2 = logl - l1;
+      if (l1 > COLS_MAX_LOG || l2 > COLS_MAX_LOG) {
+        fail("axis longer than 2^22 points");
+        return;
+      }
+      long long L1 = 1LL << l1, L2 = 1LL << l2;
+      View S = split_view(B_SCR, B_SCR, scr_base);
+      S.im.off = scr_base + outer * L;  // scratch: re block then im block
+      need_scratch(scr_base + 2 * outer * L);
+      // pass A: lines (o, t2), points t1 -> Y[o][t2][k1] (transposed store)
+      line(LK_C2C, true, true, l1, io(A, L2, 1, a_bs, l2, L2 - 1), io(S, 1, L1, L, l2, L2 - 1),
+           outer * L2, inverse, L, L2 - 1, 0);
+      // pass B: lines (o, k1), points t2 -> X[o][k1 + L1 k2]
+      line(LK_C2C, true, false, l2, io(S, L1, 1, L, l1, L1 - 1), io(B, L1, 1, b_bs, l1, L1 - 1),
+           outer * L1, inverse);
+      return;
+    }
+    int lin = ilog2ll(inner);
+    if (logl <= COLS_MAX_LOG) {
+      line(LK_C2C, true, false, logl, io(A, inner, 1, a_bs, lin, inner - 1),
+           io(B, inner, 1, b_bs, lin, inner - 1), outer * inner, inverse);
+      return;
+    }
+    // four-step along a strided axis
+    int l1 = (logl + 1) / 2, l2 = logl - l1;
+    if (l1 > COLS_MAX_LOG || l2 > COLS_MAX_LOG) {
+      fail("axis longer than 2^22 points");
+      return;
+    }
+    long long L1 = 1LL << l1, L2 = 1LL << l2;
+    long long N = outer * L * inner;
+    View S = split_view(B_SCR, B_SCR, scr_base);
+    S.im.off = scr_base + N;
+    need_scratch(scr_base + 2 * N);
+    // pass A: lines (o, t2, m), points t1 (stride L2*inner) -> Y(k1, t2, m)
+    line(LK_C2C, true, false, l1, io(A, L2 * inner, 1, a_bs, l2 + lin, L2 * inner - 1),
+         io(S, L2 * inner, 1, L * inner, l2 + lin, L2 * inner - 1), outer * L2 * inner, inverse, L,
+         L2 - 1, lin);
+    // pass B: lines (o, k1, m), points t2 (stride inner) -> X(k1 + L1 k2, m)
+    line(LK_C2C, true, false, l2, io(S, inner, 1, L2 * inner, lin, inner - 1),
+         io(B, L1 * inner, 1, b_bs, l1 + lin, L1 * inner - 1), outer * L1 * inner, inverse);
+  }
+
+  // Complex N-D transform of `count` dense arrays of shape dims[0..nd) from
+  // view A to view B: last axis first, then in place on B.
+  void nd(int nd, const long long* dims, long long count, const View& A, const View& B, bool inverse) {
+    long long total = count;
+    for (int i = 0; i < nd; i++) total *= dims[i];
+    bool first = true;
+    for (int ax = nd - 1; ax >= 0; ax--) {
+      long long L = dims[ax];
+      if (L == 1) continue;
+      long long inner = 1;
+      for (int j = ax + 1; j < nd; j++) inner *= dims[j];
+      long long outer = total / (L * inner);
+      axis(outer, L, inner, first ? A : B, B, inverse);
+      first = false;
+    }
+    if (first) {
+      // every dim is 1: copy (a length-1 transform)
+      axis(total, 1, 1, A, B, inverse);
+    }
+  }
+};
+
+std::unique_ptr<Plan> build_plan(int kind, int ndim, const long long* dims, long long batch, int format,
+                                 bool dry) {
+  std::unique_ptr<Plan> P(new Plan());
+  P->kind = kind;
+  P->format = format;
+  P->ndim = ndim;
+  for (int i = 0; i < ndim; i++) P->dims[i] = dims[i];
+  P->batch = batch;
+  if (!dry) cudaGetDevice(&P->device);
+
+  long long N = 1;
+  for (int i = 0; i < ndim; i++) N *= dims[i];
+  long long d0 = dims[0];
+  long long inner = N / d0;
+  long long H = (d0 / 2 + 1) * inner;
+  bool inter = format == 1;
+
+  View src = inter ? inter_view(B_SRC_RE) : split_view(B_SRC_RE, B_SRC_IM);
+  View dst = inter ? inter_view(B_DST_RE) : split_view(B_DST_RE, B_DST_IM);
+
+  Builder b(*P, dry);
+  if (kind == K_C || kind == K_CI) {
+    P->in_elems = N;
+    P->out_elems = N;
+    b.nd(ndim, dims, batch, src, dst, kind == K_CI);
+  } else if (ndim == 1) {
+    // 1D real: L = n/2 complex points of the interleaved view
+    long long n = d0, L = n / 2;
+    P->in_elems = kind == K_R ? n : H;
+    P->out_elems = kind == K_R ? H : n;
+    View realv = inter_view(kind == K_R ? B_SRC_RE : B_DST_RE);
+    if (n == 1) {
+      // a real transform of total size 1 (the reference crashes here):
+      // the length-1 DFT, X[0] = x[0] + 0i and x[0] = re X[0]
+      b.real1(kind == K_R, batch);
+    } else if (ilog2ll(L) <= ROWS_MAX_LOG) {
+      int logl = ilog2ll(L);
+      if (kind == K_R)
+        b.line(LK_R2C, false, false, logl, io(realv, 1, 0, L, 0, 0), io(dst, 1, 0, L + 1, 0, 0), batch,
+               false, 0, 0, 0, L);
+      else
+        b.line(LK_C2R, false, false, logl, io(src, 1, 0, L + 1, 0, 0), io(realv, 1, 0, L, 0, 0), batch,
+               false, 0, 0, 0, L);
+    } else if (kind == K_R) {
+      // complex four-step into dst lines (stride L+1), then the real pass
+      b.axis(batch, L, 1, realv, dst, false, L, L + 1);
+      b.real_pass(io(dst, 1, 0, L + 1, 0, 0), io(dst, 1, 0, L + 1, 0, 0), batch, L, false, false);
+    } else {
+      // real pre-pass into scratch (Z'), then the inverse four-step from
+      // there into dst's interleaved view, its own scratch above Z'
+      View S = split_view(B_SCR, B_SCR, 0);
+      S.im.off = batch * L;
+      b.need_scratch(2 * batch * L);
+      b.real_pass(io(src, 1, 0, L + 1, 0, 0), io(S, 1, 0, L, 0, 0), batch, L, true, false);
+      b.scr_base = 2 * batch * L;
+      b.axis(batch, L, 1, S, realv, true, L, L);
+    }
+  } else {
+    // N-D real, dim 0 halved
+    long long L = d0 / 2;
+    int logl = ilog2ll(L);
+    int lin = ilog2ll(inner);
+    P->in_elems = kind == K_R ? N : H;
+    P->out_elems = kind == K_R ? H : N;
+    // the row-pair view of the real array: z(k, m) = x[2k][m] + i x[2k+1][m]
+    // (fft_internal.hpp:281-283, multi.hpp:261-272)
+    View rows;
+    rows.re = {kind == K_R ? B_SRC_RE : B_DST_RE, 0};
+    rows.im = {kind == K_R ? B_SRC_RE : B_DST_RE, inner};
+    rows.unit = 1;
+    if (logl <= COLS_MAX_LOG) {
+      if (kind == K_R) {
+        b.line(LK_R2C, true, false, logl, io(rows, 2 * inner, 1, N, lin, inner - 1),
+               io(dst, inner, 1, H, lin, inner - 1), batch * inner, false, 0, 0, 0, L);
+        b.nd(ndim - 1, dims + 1, batch * (L + 1), dst, dst, false);
+      } else {
+        View S = split_view(B_SCR, B_SCR, 0);
+        S.im.off = batch * H;
+        b.need_scratch(2 * batch * H);
+        b.scr_base = 2 * batch * H;
+        b.nd(ndim - 1, dims + 1, batch * (L + 1), src, S, true);
+        b.line(LK_C2R, true, false, logl, io(S, inner, 1, H, lin, inner - 1),
+               io(rows, 2 * inner, 1, N, lin, inner - 1), batch * inner, false, 0, 0, 0, L);
+      }
+    } else {
+      // dim 0 too long for one CTA: pack the row pairs, four-step along
+      // dim 0, standalone real pass along dim 0 (multi.hpp:343-414)
+      long long Z = batch * L * inner;  // complex elements of the packed array
+      int ll = ilog2ll(L);
+      if (kind == K_R) {
+        View S = split_view(B_SCR, B_SCR, 0);
+        S.im.off = Z;
+        b.need_scratch(2 * Z);
+        b.copy(io(rows, 1, 2 * inner, 2 * L * inner, ll, L - 1), io(S, 1, inner, L * inner, ll, L - 1),
+               batch * L, inner);
+        b.scr_base = 2 * Z;
+        b.axis(batch, L, inner, S, dst, false, L * inner, (L + 1) * inner);
+        b.real_pass(io(dst, inner, 1, H, lin, inner - 1), io(dst, inner, 1, H, lin, inner - 1), batch * inner,
+                    L, false, true);
+        b.nd(ndim - 1, dims + 1, batch * (L + 1), dst, dst, false);
+      } else {
+        View S = split_view(B_SCR, B_SCR, 0);   // planes after the (N-1)-D inverse
+        S.im.off = batch * H;
+        View S2 = split_view(B_SCR, B_SCR, 2 * batch * H);   // Z'
+        S2.im.off = 2 * batch * H + Z;
+        View S3 = split_view(B_SCR, B_SCR, 2 * batch * H + 2 * Z);   // z
+        S3.im.off = 2 * batch * H + 3 * Z;
+        long long base = 2 * batch * H + 4 * Z;
+        b.need_scratch(base);
+        b.scr_base = base;
+        b.nd(ndim - 1, dims + 1, batch * (L + 1), src, S, true);
+        b.real_pass(io(S, inner, 1, H, lin, inner - 1), io(S2, inner, 1, L * inner, lin, inner - 1),
+                    batch * inner, L, true, true);
+        b.axis(batch, L, inner, S2, S3, true);
+        b.copy(io(S3, 1, inner, L * inner, ll, L - 1), io(rows, 1, 2 * inner, 2 * L * inner, ll, L - 1),
+               batch * L, inner);
+      }
+    }
+  }
+  if (!b.ok) {
+    set_error(1, b.err);
+    return nullptr;
+  }
+  return P;
+}
+
+static std::string io_json(const IOSpec& s) {
+  char buf[512];
+  snprintf(buf, sizeof buf,
+           "{\"re\":[%d,%lld],\"im\":[%d,%lld],\"es\":%lld,\"lo\":%lld,\"hi\":%lld,\"qshift\":%d,"
+           "\"qmask\":%lld}",
+           s.re.buf, s.re.off, s.im.buf, s.im.off, s.es, s.lo, s.hi, s.qshift, s.qmask);
+  return buf;
+}
+
+std::string describe_plan(const Plan& P) {
+  std::string o = "{";
+  char buf[1024];
+  snprintf(buf, sizeof buf,
+           "\"kind\":%d,\"format\":%d,\"batch\":%lld,\"in_elems\":%lld,\"out_elems\":%lld,"
+           "\"scratch_floats\":%lld,\"ops\":[",
+           P.kind, P.format, P.batch, P.in_elems, P.out_elems, P.scratch_floats);
+  o += buf;
+  for (size_t i = 0; i < P.ops.size(); i++) {
+    const Op& op = P.ops[i];
+    if (i) o += ",";
+    if (op.type == OP_LINE) {
+      snprintf(buf, sizeof buf,
+               "{\"type\":\"line\",\"logl\":%d,\"cols\":%d,\"lk\":%d,\"tstore\":%d,\"C\":%d,"
+               "\"threads\":%d,\"smem\":%zu,\"grid\":%lld,\"nlines\":%lld,\"inverse\":%d,"
+               "\"tw_n\":%lld,\"tw_qmask\":%lld,\"tw_qshift\":%d,\"real_L\":%lld,",
+               op.k.logl, op.k.cols, op.k.kind, op.k.tstore, op.k.lines_per_cta, op.threads, op.smem, op.grid,
+               op.p.nlines, op.p.inverse, op.p.tw_n, op.p.tw_qmask, op.p.tw_qshift, op.real_L);
+    } else if (op.type == OP_REAL) {
+      snprintf(buf, sizeof buf,
+               "{\"type\":\"real\",\"threads\":%d,\"grid\":%lld,\"nlines\":%lld,\"L\":%lld,"
+               "\"inverse\":%d,\"lines_fastest\":%d,",
+               op.threads, op.grid, op.rp.nlines, op.rp.L, op.rp.inverse, op.rp.lines_fastest);
+    } else if (op.type == OP_COPY) {
+      snprintf(buf, sizeof buf, "{\"type\":\"copy\",\"threads\":%d,\"grid\":%lld,\"nlines\":%lld,\"len\":%lld,",
+               op.threads, op.grid, op.cp.nlines, op.cp.len);
+    } else {
+      snprintf(buf, sizeof buf, "{\"type\":\"real1\",\"threads\":%d,\"grid\":%lld,\"nlines\":%lld,\"inverse\":%d,",
+               op.threads, op.grid, op.rp.nlines, op.rp.inverse);
+    }
+    o += buf;
+    o += "\"in\":" + io_json(op.in) + ",\"out\":" + io_json(op.out) + "}";
+  }
+  o += "]}";
+  return o;
+}
+
+Plan::~Plan() {
+  if (scratch) cudaFree(scratch);
+  if (stage) cudaFree(stage);
+  if (stream) cudaStreamDestroy(stream);
+}
+
+static inline float* resolve(const Ref& r, float* const* base) { return base[r.buf] ? base[r.buf] + r.off : nullptr; }
+
+static LineIO bind(const IOSpec& s, float* const* base) {
+  LineIO o;
+  o.re = resolve(s.re, base);
+  o.im = resolve(s.im, base);
+  o.es = s.es;
+  o.lo = s.lo;
+  o.hi = s.hi;
+  o.qshift = s.qshift;
+  o.qmask = s.qmask;
+  return o;
+}
+
+int Plan::launch(const float* src_re, const float* src_im, float* dst_re, float* dst_im, cudaStream_t st) {
+  if (scratch_floats > 0 && !scratch) {
+    if (cudaMalloc(&scratch, (size_t)scratch_floats * sizeof(float)) != cudaSuccess) {
+      cudaGetLastError();
+      set_error(3, "scratch allocation failed");
+      return 3;
+    }
+  }
+  float* base[B_NBUF] = {(float*)src_re, (float*)src_im, dst_re, dst_im, scratch};
+  for (auto& op : ops) {
+    if (op.type == OP_LINE) {
+      LineParams p = op.p;
+      p.in = bind(op.in, base);
+      p.out = bind(op.out, base);
+      if (op.smem > 48 * 1024) {
+        cudaFuncSetAttribute((const void*)op.k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)op.smem);
+      }
+      op.k.fn<<<(unsigned)op.grid, op.threads, op.smem, st>>>(p);
+    } else if (op.type == OP_REAL) {
+      RealPassParams rp = op.rp;
+      rp.in = bind(op.in, base);
+      rp.out = bind(op.out, base);
+      real_pass_kernel<<<(unsigned)op.grid, op.threads, 0, st>>>(rp);
+    } else if (op.type == OP_COPY) {
+      CopyParams cp = op.cp;
+      cp.in = bind(op.in, base);
+      cp.out = bind(op.out, base);
+      copy_lines_kernel<<<(unsigned)op.grid, op.threads, 0, st>>>(cp);
+    } else {
+      RealPassParams rp = op.rp;
+      rp.in = bind(op.in, base);
+      rp.out = bind(op.out, base);
+      real1_kernel<<<(unsigned)op.grid, op.threads, 0, st>>>(rp);
+    }
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error(4, std::string("kernel launch failed: ") + cudaGetErrorString(e));
+    return 4;
+  }
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// kernel registry
+// ---------------------------------------------------------------------------
+bool get_line_kernel(int logl, bool cols, int kind, bool tstore, LineKernel* out) {
+  if (logl < 0) return false;
+  if (!cols) {
+    if (tstore || logl > ROWS_MAX_LOG) return false;
+    if (kind == LK_C2C) return get_rows_c2c(logl, out);
+    if (kind == LK_R2C) return get_rows_r2c(logl, out);
+    if (kind == LK_C2R) return get_rows_c2r(logl, out);
+    return false;
+  }
+  if (logl > COLS_MAX_LOG) return false;
+  if (kind == LK_C2C) return get_cols_c2c(logl, tstore, out);
+  if (tstore) return false;
+  return get_cols_real(logl, kind, out);
+}
+
+int validate_shape(int ndim, const size_t* dim, int* ndim_out, long long* dims_out) {
+  if (ndim > 64) return 1;
+  int k = 0;
+  long long total = 1;
+  for (int i = 0; i < ndim; i++) {
+    size_t d = dim[i];
+    if (d == 0 || (d & (d - 1)) != 0) return 1;
+    if (d > (1ULL << 31)) return 1;
+    total *= (long long)d;
+    if (total > (1LL << 31)) return 1;
+    if (d != 1) dims_out[k++] = (long long)d;
+  }
+  if (k == 0) dims_out[k++] = 1;
+  *ndim_out = k;
+  return 0;
+}
+
+}  // namespace agb

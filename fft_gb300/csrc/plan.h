@@ -1,0 +1,96 @@
+// Host-side plans: a transform is compiled into a short list of kernel
+// launches ("ops") over named buffers; executing a plan binds the buffers to
+// the caller's pointers and launches the ops on one stream.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "kernels.h"
+
+namespace agb {
+
+enum Kind { K_C = 0, K_CI = 1, K_R = 2, K_RI = 3 };
+
+// Buffers an op reads or writes.  Data pointers are bound at execution.
+enum BufId { B_SRC_RE = 0, B_SRC_IM, B_DST_RE, B_DST_IM, B_SCR, B_NBUF };
+
+struct Ref {
+  int buf = B_SRC_RE;
+  long long off = 0;  // floats from the buffer base
+};
+
+struct IOSpec {
+  Ref re, im;
+  long long es = 1, lo = 0, hi = 0;
+  int qshift = 0;
+  long long qmask = 0;
+};
+
+enum OpType { OP_LINE = 0, OP_REAL = 1, OP_REAL1 = 2, OP_COPY = 3 };
+
+struct Op {
+  int type = OP_LINE;
+  LineKernel k{};
+  LineParams p{};
+  RealPassParams rp{};
+  CopyParams cp{};
+  IOSpec in, out;
+  long long real_L = 0;  // real twiddle length of a fused line op
+  long long grid = 0;
+  int threads = 0;
+  size_t smem = 0;
+};
+
+// Error state of the calling thread.
+void set_error(int code, const std::string& msg);
+void clear_error();
+
+struct Plan {
+  int kind = K_C;
+  int format = 0;              // afft_split / afft_interleaved
+  int ndim = 1;
+  long long dims[64] = {0};
+  long long batch = 1;
+  long long in_elems = 0;      // complex (or real) elements per array, one transform
+  long long out_elems = 0;
+  int device = 0;
+  std::vector<Op> ops;
+  long long scratch_floats = 0;
+  long long real_L_of_op = 0;
+  float* scratch = nullptr;
+  cudaStream_t stream = nullptr;
+  // device staging for host-resident data
+  float* stage = nullptr;
+  size_t stage_bytes = 0;
+  std::mutex mu;
+
+  ~Plan();
+  // Launch all ops on `stream`; pointers must be device-accessible.
+  int launch(const float* src_re, const float* src_im, float* dst_re, float* dst_im,
+             cudaStream_t stream);
+};
+
+// Build a plan; returns nullptr and sets the error on failure.
+// dry: build the op list only (no device calls, twiddle pointers null), for
+// describing a plan without a GPU.
+std::unique_ptr<Plan> build_plan(int kind, int ndim, const long long* dims, long long batch,
+                                 int format, bool dry = false);
+
+// JSON description of a plan's ops (kernel shapes, grids, address specs).
+std::string describe_plan(const Plan& P);
+
+// Validation shared by memsize and create: 0 on success, else error code.
+int validate_shape(int ndim, const size_t* dim, int* ndim_out, long long* dims_out);
+
+// Device twiddle tables (FP64-computed, rounded once), cached per device.
+const float2* stage_twiddles(int logl);
+const float2* real_twiddles(long long L);         // W_{2L}^k, k < L
+void fourstep_tables(long long N, const float2** hi, const float2** lo, int* lo_bits);
+
+}  // namespace agb

@@ -1,0 +1,232 @@
+"""CPU emulation of a libafft_gb300 plan, for checking the host logic without a
+GPU.
+
+``describe(kind, dims, batch, fmt)`` returns the library's own JSON
+description of the kernel launches a plan issues (afft_gb300_plan_describe,
+no device calls).  ``run(desc, ...)`` executes those launches on float64
+numpy buffers: every launch gathers and scatters through exactly the address
+formulas the kernels use (off(q) = (q >> qshift) * hi + (q & qmask) * lo,
+element stride es), applies the math each kernel type computes (a length-L
+DFT per line with the four-step twiddle, the fused real post/pre pass, the
+standalone real pass, the packing copy), and checks on the way that
+
+* every address lies inside its buffer,
+* no address is written twice within a launch,
+* when a launch reads and writes the same buffer, no CTA writes an address
+  that another CTA reads (the kernels rely on this to run in place).
+
+The Stockham stages inside a kernel are not emulated (a line's DFT is taken
+with numpy); those are checked on the GPU against the oracle.
+"""
+import ctypes
+import json
+
+import numpy as np
+
+import fft_gb300 as G
+
+SRC_RE, SRC_IM, DST_RE, DST_IM, SCR = range(5)
+
+
+def describe(kind, dims, batch=1, fmt=0):
+    L = G.lib()
+    f = L.afft_gb300_plan_describe
+    f.restype = ctypes.c_size_t
+    f.argtypes = [ctypes.c_int, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int,
+                  ctypes.c_char_p, ctypes.c_size_t]
+    k = G.KINDS[kind] if isinstance(kind, str) else kind
+    arr = (ctypes.c_size_t * max(1, len(dims)))(*dims)
+    n = f(k, len(dims), arr, batch, fmt, None, 0)
+    if n == 0:
+        raise ValueError(G.last_error())
+    buf = ctypes.create_string_buffer(n)
+    f(k, len(dims), arr, batch, fmt, buf, n)
+    return json.loads(buf.value.decode())
+
+
+def w(m, n):
+    """exp(-2 pi i m / n) in float64."""
+    return np.exp(-2j * np.pi * (np.asarray(m, np.float64) % n) / n)
+
+
+class Buffers:
+    def __init__(self, sizes):
+        self.b = [None if s is None else np.full(s, np.nan) for s in sizes]
+
+    def addr(self, ref, idx):
+        buf, off = ref
+        a = off + idx
+        arr = self.b[buf]
+        assert arr is not None, "launch touches an unbound buffer %d" % buf
+        assert a.min() >= 0 and a.max() < arr.size, "out of bounds on buffer %d: [%d, %d] of %d" % (
+            buf, a.min(), a.max(), arr.size)
+        return buf, a
+
+
+def line_offsets(spec, q):
+    return (q >> spec["qshift"]) * spec["hi"] + (q & spec["qmask"]) * spec["lo"]
+
+
+class Access:
+    """Records reads/writes of one launch, per buffer, with the CTA id."""
+
+    def __init__(self):
+        self.reads = {}
+        self.writes = {}
+
+    def note(self, table, buf, addrs, cta):
+        addrs = np.asarray(addrs)
+        cta = np.broadcast_to(np.asarray(cta), addrs.shape)
+        table.setdefault(buf, []).append((addrs.reshape(-1), cta.reshape(-1)))
+
+    def check(self):
+        for buf, lst in self.writes.items():
+            a = np.concatenate([x for x, _ in lst])
+            c = np.concatenate([y for _, y in lst])
+            u, cnt = np.unique(a, return_counts=True)
+            assert cnt.max() == 1, "address written twice in one launch (buffer %d)" % buf
+            if buf in self.reads:
+                ra = np.concatenate([x for x, _ in self.reads[buf]])
+                rc = np.concatenate([y for _, y in self.reads[buf]])
+                order = np.argsort(a)
+                a_s, c_s = a[order], c[order]
+                pos = np.searchsorted(a_s, ra)
+                hit = (pos < a_s.size)
+                hit[hit] &= a_s[pos[hit]] == ra[hit]
+                bad = hit.copy()
+                bad[hit] = c_s[pos[hit]] != rc[hit]
+                assert not bad.any(), "CTA reads an address another CTA writes (buffer %d)" % buf
+
+
+def _gather(B, acc, spec, q, idx, cta):
+    ore = line_offsets(spec, q)[:, None] + idx[None, :] * spec["es"]
+    bre, are = B.addr(spec["re"], ore)
+    bim, aim = B.addr(spec["im"], ore)
+    ctas = np.broadcast_to(cta[:, None], ore.shape)
+    acc.note(acc.reads, bre, are, ctas)
+    acc.note(acc.reads, bim, aim, ctas)
+    return B.b[bre][are] + 1j * B.b[bim][aim]
+
+
+def _scatter(B, acc, spec, q, idx, cta, val):
+    ore = line_offsets(spec, q)[:, None] + idx[None, :] * spec["es"]
+    bre, are = B.addr(spec["re"], ore)
+    bim, aim = B.addr(spec["im"], ore)
+    ctas = np.broadcast_to(cta[:, None], ore.shape)
+    acc.note(acc.writes, bre, are, ctas)
+    acc.note(acc.writes, bim, aim, ctas)
+    return (bre, are, val.real), (bim, aim, val.imag)
+
+
+def _scatter_re(B, acc, spec, q, idx, cta, val):
+    ore = line_offsets(spec, q)[:, None] + idx[None, :] * spec["es"]
+    bre, are = B.addr(spec["re"], ore)
+    acc.note(acc.writes, bre, are, np.broadcast_to(cta[:, None], ore.shape))
+    return (bre, are, val.real),
+
+
+def run_op(B, op):
+    acc = Access()
+    pending = []
+    t = op["type"]
+    if t == "line":
+        L = 1 << op["logl"]
+        q = np.arange(op["nlines"], dtype=np.int64)
+        cta = q // op["C"]
+        lk = op["lk"]
+        if lk == 2:  # C2R: reads L+1 bins
+            X = _gather(B, acc, op["in"], q, np.arange(L + 1), cta)
+            i = np.arange(L)
+            s0, s1 = X[:, i], X[:, L - i]
+            wv = w(i, 2 * L)
+            a = s0 + np.conj(s1)
+            b = (np.conj(s1) - s0) * np.conj(wv)
+            Zp = a - 1j * b
+            Zp[:, 0] = (X[:, 0].real + X[:, L].real) + 1j * (X[:, 0].real - X[:, L].real)
+            z = np.fft.ifft(Zp, axis=1) * L
+            pending += _scatter(B, acc, op["out"], q, np.arange(L), cta, z)
+        else:
+            x = _gather(B, acc, op["in"], q, np.arange(L), cta)
+            Xf = np.fft.ifft(x, axis=1) * L if op["inverse"] else np.fft.fft(x, axis=1)
+            if op["tw_n"]:
+                col = (q >> op["tw_qshift"]) & op["tw_qmask"]
+                tw = w(col[:, None] * np.arange(L)[None, :], op["tw_n"])
+                Xf = Xf * (np.conj(tw) if op["inverse"] else tw)
+            if lk == 0:
+                pending += _scatter(B, acc, op["out"], q, np.arange(L), cta, Xf)
+            else:  # R2C post pass: L+1 bins
+                k = np.arange(L + 1)
+                s0 = Xf[:, k % L]
+                s1 = Xf[:, (L - k) % L]
+                out = (s0 + np.conj(s1)) / 2 - 0.5j * w(k, 2 * L) * (s0 - np.conj(s1))
+                out[:, 0] = Xf[:, 0].real + Xf[:, 0].imag
+                out[:, L] = Xf[:, 0].real - Xf[:, 0].imag
+                pending += _scatter(B, acc, op["out"], q, k, cta, out)
+    elif t == "real":
+        L = op["L"]
+        q = np.arange(op["nlines"], dtype=np.int64)
+        cta = q  # one thread per pair: reads and writes stay in a thread
+        # the kernel's k = 0 thread also reads slot L in both directions
+        X = _gather(B, acc, op["in"], q, np.arange(L + 1), cta)
+        k = np.arange(L + 1) if not op["inverse"] else np.arange(L)
+        if not op["inverse"]:
+            Z = X[:, :L]
+            s0, s1 = Z[:, k % L], Z[:, (L - k) % L]
+            out = (s0 + np.conj(s1)) / 2 - 0.5j * w(k, 2 * L) * (s0 - np.conj(s1))
+            out[:, 0] = Z[:, 0].real + Z[:, 0].imag
+            out[:, L] = Z[:, 0].real - Z[:, 0].imag
+        else:
+            s0, s1 = X[:, k], X[:, L - k]
+            out = (s0 + np.conj(s1)) - 1j * (np.conj(s1) - s0) * np.conj(w(k, 2 * L))
+            out[:, 0] = (X[:, 0].real + X[:, L].real) + 1j * (X[:, 0].real - X[:, L].real)
+        pending += _scatter(B, acc, op["out"], q, k, cta, out)
+    elif t == "copy":
+        q = np.arange(op["nlines"], dtype=np.int64)
+        cta = np.zeros_like(q)  # copies never run in place
+        x = _gather(B, acc, op["in"], q, np.arange(op["len"]), cta)
+        pending += _scatter(B, acc, op["out"], q, np.arange(op["len"]), cta, x)
+    elif t == "real1":
+        q = np.arange(op["nlines"], dtype=np.int64)
+        x = _gather(B, acc, op["in"], q, np.arange(1), q)
+        if op["inverse"]:
+            pending += _scatter_re(B, acc, op["out"], q, np.arange(1), q, x.real + 0j)
+        else:
+            pending += _scatter(B, acc, op["out"], q, np.arange(1), q, x.real + 0j)
+    else:
+        raise ValueError(t)
+    acc.check()
+    for buf, addr, val in pending:
+        B.b[buf][addr] = val
+
+
+def buffer_sizes(desc):
+    kind, fmt, batch = desc["kind"], desc["format"], desc["batch"]
+    ie, oe = desc["in_elems"] * batch, desc["out_elems"] * batch
+    inter = fmt == 1
+    cin = kind != 2      # complex input
+    cout = kind != 3     # complex output
+    src_re = ie * (2 if (inter and cin) else 1)
+    src_im = ie if (cin and not inter) else None
+    dst_re = oe * (2 if (inter and cout) else 1)
+    dst_im = oe if (cout and not inter) else None
+    return [src_re, src_im, dst_re, dst_im, desc["scratch_floats"] or None]
+
+
+def run(desc, a, b=None):
+    """Execute a described plan on inputs (split arrays); returns outputs as
+    split arrays (re, im) or the real array."""
+    B = Buffers(buffer_sizes(desc))
+    kind, inter = desc["kind"], desc["format"] == 1
+    if kind == 2:
+        B.b[SRC_RE][:] = a
+    elif inter:
+        B.b[SRC_RE][0::2], B.b[SRC_RE][1::2] = a, b
+    else:
+        B.b[SRC_RE][:], B.b[SRC_IM][:] = a, b
+    for op in desc["ops"]:
+        run_op(B, op)
+    if kind == 3:
+        return B.b[DST_RE].copy()
+    if inter:
+        return B.b[DST_RE][0::2].copy(), B.b[DST_RE][1::2].copy()
+    return B.b[DST_RE].copy(), B.b[DST_IM].copy()

@@ -1,0 +1,320 @@
+"""GPU parity: every transform through the C ABI (libafft_gb300.so) against
+the FP64 oracle (testing.cpp:870-1002 restated) and the reference afft
+library's own float outputs (tests/golden).
+
+Tolerance (plain FP32 path): relative L2 error <= 2e-6 against the FP64
+oracle, and <= 2e-6 against afft's float output on the same input; the
+unnormalised round trip inverse(forward(x))/n recovers x to 2e-6.
+"""
+import numpy as np
+import pytest
+
+import fft_gb300 as G
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL = 2e-6
+
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def dev():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch.device("cuda:0")
+
+
+def to_dev(a, dev, pad=0):
+    """Copy to a device tensor, optionally starting `pad` floats into the
+    allocation (unaligned pointers)."""
+    t = torch.zeros(a.size + pad + 1, dtype=torch.float32, device=dev)
+    t[pad:pad + a.size] = torch.from_numpy(np.ascontiguousarray(a, np.float32))
+    return t[pad:pad + a.size]
+
+
+def run_plan(kind, dims, a, b, dev, fmt=G.afft_split, host=False, pad=0, inplace=False):
+    """One transform through the fft.h entry points; returns numpy output
+    (tuple for complex outputs)."""
+    cls = {"c": G.complex_transform, "ci": G.inverse_complex_transform,
+           "r": G.real_transform, "ri": G.inverse_real_transform}[kind]
+    plan = cls(dims, fmt=fmt)
+    n = int(np.prod(dims))
+    h = O.half_elems(dims)
+    out_n = {"c": n, "ci": n, "r": h, "ri": n}[kind]
+    inter = fmt == G.afft_interleaved
+    if host:
+        conv = lambda x: np.ascontiguousarray(x, np.float32)
+        zeros = lambda m: np.zeros(m, np.float32)
+        back = lambda x: x
+    else:
+        conv = lambda x: to_dev(x, dev, pad)
+        zeros = lambda m: torch.zeros(m, dtype=torch.float32, device=dev)
+        back = lambda x: x.cpu().numpy()
+    if kind in ("c", "ci"):
+        if inter:
+            src = np.empty(2 * n, np.float32)
+            src[0::2], src[1::2] = a, b
+            s = conv(src)
+            d = s if inplace else zeros(2 * n)
+            plan(s, None, d, None)
+            o = back(d)
+            return o[0::2].copy(), o[1::2].copy()
+        sr, si = conv(a), conv(b)
+        if inplace:
+            dr, di = sr, si
+        else:
+            dr, di = zeros(n), zeros(n)
+        plan(sr, si, dr, di)
+        return back(dr), back(di)
+    if kind == "r":
+        s = conv(a)
+        if inter:
+            d = zeros(2 * h)
+            plan(s, d, None)
+            o = back(d)
+            return o[0::2].copy(), o[1::2].copy()
+        dr, di = zeros(h), zeros(h)
+        plan(s, dr, di)
+        return back(dr), back(di)
+    if inter:
+        src = np.empty(2 * h, np.float32)
+        src[0::2], src[1::2] = a, b
+        s = conv(src)
+        d = zeros(n)
+        plan(s, None, d)
+        return back(d)
+    sr, si = conv(a), conv(b)
+    d = zeros(n)
+    plan(sr, si, d)
+    return back(d)
+
+
+def inputs(kind, dims, seed):
+    n = int(np.prod(dims))
+    h = O.half_elems(dims)
+    rng = np.random.default_rng(seed)
+    if kind in ("c", "ci"):
+        return rng.uniform(-1, 1, n).astype(np.float32), rng.uniform(-1, 1, n).astype(np.float32)
+    if kind == "r":
+        return rng.standard_normal(n).astype(np.float32), None
+    return rng.standard_normal(h).astype(np.float32), rng.standard_normal(h).astype(np.float32)
+
+
+def check(kind, dims, a, b, got, tol=TOL):
+    ref = O.oracle64(kind, dims, a, b)
+    err = O.rel_l2(got, ref)
+    assert err <= tol, (kind, dims, err)
+    return err
+
+
+# --- the reference's own outputs ----------------------------------------------
+
+def test_golden_cases(golden, dev):
+    z, cases = golden
+    worst = 0.0
+    for case in cases:
+        nm, kind, dims = case["name"], case["kind"], case["dims"]
+        if nm == "c1":
+            continue
+        a = z[nm + "/in0"]
+        b = z[nm + "/in1"] if nm + "/in1" in z else None
+        got = run_plan(kind, dims, a, b, dev)
+        worst = max(worst, check(kind, dims, a, b, got))
+        for tag in ("scalar", "auto"):
+            ref = z[nm + "/%s0" % tag] if kind == "ri" else (z[nm + "/%s0" % tag], z[nm + "/%s1" % tag])
+            err = O.rel_l2(got, ref)
+            assert err <= TOL, (nm, tag, err)
+    print("worst rel-L2 vs FP64 over golden cases: %.2e" % worst)
+
+
+def test_c1_harness_input_and_round_trip(golden, dev):
+    z, _ = golden
+    a, b = z["c1/in0"], z["c1/in1"]
+    fr, fi = run_plan("c", [1024], a, b, dev)
+    assert O.rel_l2((fr, fi), (z["c1/auto0"], z["c1/auto1"])) <= TOL
+    check("c", [1024], a, b, (fr, fi))
+    br, bi = run_plan("ci", [1024], fr, fi, dev)
+    assert O.rel_l2((br / 1024, bi / 1024), (a, b)) <= TOL
+    assert O.rel_l2((br / 1024, bi / 1024), (z["c1/auto_inv0"], z["c1/auto_inv1"])) <= TOL
+
+
+def test_golden_host_pointers(golden, dev):
+    # afft callers pass host memory: the library stages it
+    z, cases = golden
+    for case in cases[::7]:
+        nm, kind, dims = case["name"], case["kind"], case["dims"]
+        if nm == "c1":
+            continue
+        a = z[nm + "/in0"]
+        b = z[nm + "/in1"] if nm + "/in1" in z else None
+        check(kind, dims, a, b, run_plan(kind, dims, a, b, dev, host=True))
+
+
+# --- shapes beyond the fixtures ---------------------------------------------
+
+ONE_D = [2 ** k for k in range(0, 21)]
+
+
+@pytest.mark.parametrize("n", ONE_D)
+@pytest.mark.parametrize("kind", ["c", "ci", "r", "ri"])
+def test_1d_all_sizes(kind, n, dev):
+    if kind in ("r", "ri") and n == 1:
+        pytest.skip("covered by test_real_size_one")
+    a, b = inputs(kind, [n], n + len(kind))
+    check(kind, [n], a, b, run_plan(kind, [n], a, b, dev))
+
+
+ND = [[2, 2], [4, 64], [64, 4], [256, 256], [32, 4096], [4096, 32], [8, 16384], [16384, 8], [4, 65536],
+      [8192, 4], [16384, 16, 2], [2, 2, 2], [16, 32, 64], [64, 64, 64], [8, 2048, 8], [4, 4, 4, 4, 4],
+      [2, 8, 2, 8, 2, 8], [1, 512, 1, 16], [2048, 16]]
+
+
+@pytest.mark.parametrize("dims", ND, ids=lambda d: "x".join(map(str, d)))
+@pytest.mark.parametrize("kind", ["c", "ci", "r", "ri"])
+def test_nd(kind, dims, dev):
+    a, b = inputs(kind, dims, sum(dims) + len(kind))
+    check(kind, dims, a, b, run_plan(kind, dims, a, b, dev))
+
+
+@pytest.mark.parametrize("dims", [[16], [1024], [65536], [8, 64], [64, 8, 4], [4096, 4]], ids=str)
+@pytest.mark.parametrize("kind", ["c", "ci", "r", "ri"])
+def test_interleaved_format(kind, dims, dev):
+    a, b = inputs(kind, dims, 3)
+    check(kind, dims, a, b, run_plan(kind, dims, a, b, dev, fmt=G.afft_interleaved))
+
+
+@pytest.mark.parametrize("dims", [[4096], [1 << 17], [16, 256], [128, 8192]], ids=str)
+def test_in_place_complex(dims, dev):
+    for kind in ("c", "ci"):
+        a, b = inputs(kind, dims, 5)
+        check(kind, dims, a, b, run_plan(kind, dims, a, b, dev, inplace=True))
+        check(kind, dims, a, b, run_plan(kind, dims, a, b, dev, fmt=G.afft_interleaved, inplace=True))
+
+
+@pytest.mark.parametrize("kind", ["c", "ci", "r", "ri"])
+def test_unaligned_pointers(kind, dev):
+    # the reference harness shifts buffers off alignment (testing.cpp:67-90)
+    for dims in ([1024], [64, 32], [1 << 16]):
+        a, b = inputs(kind, dims, 11)
+        check(kind, dims, a, b, run_plan(kind, dims, a, b, dev, pad=1))
+        check(kind, dims, a, b, run_plan(kind, dims, a, b, dev, pad=3))
+
+
+def test_real_size_one(dev):
+    # the reference crashes on a real transform of total size 1; here it is
+    # the length-1 DFT
+    x = np.array([0.75], np.float32)
+    re, im = run_plan("r", [1, 1], x, None, dev)
+    assert re[0] == np.float32(0.75) and im[0] == 0.0
+    y = run_plan("ri", [1], np.array([1.5], np.float32), np.array([-2.0], np.float32), dev)
+    assert y[0] == np.float32(1.5)
+
+
+def test_round_trips(dev):
+    rng = np.random.default_rng(2)
+    for dims in ([4096], [1 << 18], [256, 256], [32, 32, 32]):
+        n = int(np.prod(dims))
+        xr = rng.standard_normal(n).astype(np.float32)
+        xi = rng.standard_normal(n).astype(np.float32)
+        fr, fi = run_plan("c", dims, xr, xi, dev)
+        br, bi = run_plan("ci", dims, fr, fi, dev)
+        assert O.rel_l2((br / n, bi / n), (xr, xi)) <= TOL
+        hr, hi = run_plan("r", dims, xr, None, dev)
+        y = run_plan("ri", dims, hr, hi, dev)
+        assert O.rel_l2(y / n, xr) <= TOL
+
+
+# --- batched extension ---------------------------------------------------------
+
+@pytest.mark.parametrize("kind", ["c", "ci", "r", "ri"])
+@pytest.mark.parametrize("dims,batch", [([64], 37), ([4096], 9), ([1 << 16], 3), ([16, 64], 5), ([8, 8, 8], 7)],
+                         ids=str)
+def test_batch_plan(kind, dims, batch, dev):
+    n = int(np.prod(dims))
+    h = O.half_elems(dims)
+    in_n = {"c": n, "ci": n, "r": n, "ri": h}[kind]
+    out_n = {"c": n, "ci": n, "r": h, "ri": n}[kind]
+    rng = np.random.default_rng(batch)
+    a = rng.standard_normal(in_n * batch).astype(np.float32)
+    b = None if kind == "r" else rng.standard_normal(in_n * batch).astype(np.float32)
+    plan = G.BatchPlan(kind, dims, batch)
+    da = torch.from_numpy(a).to(dev)
+    db = None if b is None else torch.from_numpy(b).to(dev)
+    oa = torch.zeros(out_n * batch, device=dev)
+    ob = None if kind == "ri" else torch.zeros(out_n * batch, device=dev)
+    if kind in ("c", "ci"):
+        plan(da, db, oa, ob)
+    elif kind == "r":
+        plan(da, oa, ob)
+    else:
+        plan(da, db, oa)
+    oa = oa.cpu().numpy()
+    ob = None if ob is None else ob.cpu().numpy()
+    for j in range(batch):
+        si, so = slice(j * in_n, (j + 1) * in_n), slice(j * out_n, (j + 1) * out_n)
+        got = oa[so] if kind == "ri" else (oa[so], ob[so])
+        check(kind, dims, a[si], None if b is None else b[si], got)
+
+
+def test_async_on_stream(dev):
+    n, batch = 4096, 16
+    rng = np.random.default_rng(4)
+    xr = torch.from_numpy(rng.standard_normal(n * batch).astype(np.float32)).to(dev)
+    xi = torch.from_numpy(rng.standard_normal(n * batch).astype(np.float32)).to(dev)
+    yr, yi = torch.empty_like(xr), torch.empty_like(xi)
+    plan = G.BatchPlan("c", [n], batch)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        plan.launch(xr, xi, yr, yi, stream=s)
+    s.synchronize()
+    a, b = xr.cpu().numpy(), xi.cpu().numpy()
+    got = (yr.cpu().numpy()[:n], yi.cpu().numpy()[:n])
+    check("c", [n], a[:n], b[:n], got)
+
+
+def test_plan_lifecycle(dev):
+    p = G.complex_transform([256])
+    state = p.state
+    assert p.launches == 1
+    p.release()
+    # a released plan is reported, not used
+    assert G.lib().afft_gb300_plan_launches(state) == -1
+
+
+def test_errors_with_device(dev):
+    with pytest.raises(G.AfftError):
+        G.complex_transform([12])
+    assert G.last_error()[0] == 1
+    with pytest.raises(G.AfftError):
+        G.complex_transform([16], impl=G.afft_scalar)
+    assert G.supported(G.afft_auto) and G.supported(G.afft_gb300)
+    assert not G.supported(G.afft_avx2)
+
+
+def test_queue_mixed(dev):
+    rng = np.random.default_rng(9)
+    specs = [("c", [64]), ("ci", [4096]), ("r", [1024]), ("ri", [256]), ("c", [16, 32]), ("r", [8, 8, 8]),
+             ("ri", [64, 16]), ("c", [1 << 15]), ("c", [64])]
+    items, host = [], []
+    for kind, dims in specs:
+        n = int(np.prod(dims))
+        h = O.half_elems(dims)
+        in_n = {"c": n, "ci": n, "r": n, "ri": h}[kind]
+        out_n = {"c": n, "ci": n, "r": h, "ri": n}[kind]
+        a = rng.standard_normal(in_n).astype(np.float32)
+        b = None if kind == "r" else rng.standard_normal(in_n).astype(np.float32)
+        da = torch.from_numpy(a).to(dev)
+        db = None if b is None else torch.from_numpy(b).to(dev)
+        oa = torch.zeros(out_n, device=dev)
+        ob = None if kind == "ri" else torch.zeros(out_n, device=dev)
+        items.append((kind, dims, da, db, oa, ob))
+        host.append((kind, dims, a, b))
+    q = G.Queue(items)
+    for _ in range(2):
+        q.run()
+        torch.cuda.synchronize()
+        for (kind, dims, a, b), it in zip(host, items):
+            got = it[4].cpu().numpy() if kind == "ri" else (it[4].cpu().numpy(), it[5].cpu().numpy())
+            check(kind, dims, a, b, got)

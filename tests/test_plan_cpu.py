@@ -1,0 +1,63 @@
+"""Host logic without a GPU: the launch plans the library builds (described
+by afft_gb300_plan_describe, no device calls) are executed by the numpy plan
+emulator, which checks every address against its buffer and every in-place
+launch for cross-CTA hazards, and must reproduce the FP64 oracle."""
+import numpy as np
+import pytest
+
+import fft_gb300 as G
+from oracle import oracle as O
+from plan_emulator import describe, run
+
+SHAPES = [[1], [2], [4], [16], [32], [256], [4096], [16384], [32768], [1 << 16], [1 << 19],
+          [2, 2], [4, 8], [64, 4], [8, 4096], [4096, 8], [16, 2048, 2], [8192, 4], [2, 16384],
+          [2, 4, 8], [16, 16, 16], [4, 4, 4, 4], [2, 2, 2, 2, 2], [1, 32, 1], [4, 1, 1, 8]]
+
+
+def _inputs(kind, dims, batch, seed):
+    n = int(np.prod(dims))
+    h = O.half_elems(dims)
+    m = (n if kind in ("c", "ci", "r") else h) * batch
+    rng = np.random.default_rng(seed)
+    a = rng.standard_normal(m)
+    b = None if kind == "r" else rng.standard_normal(m)
+    return a, b
+
+
+def _expected(kind, dims, batch, a, b):
+    n = int(np.prod(dims))
+    h = O.half_elems(dims)
+    m_in = n if kind in ("c", "ci", "r") else h
+    outs = []
+    for j in range(batch):
+        s = slice(j * m_in, (j + 1) * m_in)
+        outs.append(O.oracle64(kind, dims, a[s], None if b is None else b[s]))
+    if kind == "ri":
+        return np.concatenate(outs)
+    return np.concatenate([o[0] for o in outs]), np.concatenate([o[1] for o in outs])
+
+
+@pytest.mark.parametrize("dims", SHAPES, ids=lambda d: "x".join(map(str, d)))
+@pytest.mark.parametrize("kind", ["c", "ci", "r", "ri"])
+def test_plan_emulation(kind, dims):
+    n = int(np.prod(dims))
+    if kind in ("r", "ri") and n == 1:
+        dims = [1]
+    for fmt in (G.afft_split, G.afft_interleaved):
+        for batch in (1, 3):
+            if n * batch > (1 << 20) and batch > 1:
+                continue
+            desc = describe(kind, dims, batch, fmt)
+            a, b = _inputs(kind, dims, batch, n + batch)
+            got = run(desc, a, b)
+            ref = _expected(kind, dims, batch, a, b)
+            assert O.rel_l2(got, ref) < 1e-12, (kind, dims, batch, fmt)
+
+
+def test_launch_counts():
+    # one pass while a line fits one CTA, two (four-step) beyond
+    assert len(describe("c", [4096], 16384)["ops"]) == 1
+    assert len(describe("c", [1 << 16], 4)["ops"]) == 2
+    assert len(describe("c", [256, 256, 256])["ops"]) == 3
+    assert len(describe("r", [4096, 4096])["ops"]) == 2
+    assert len(describe("r", [1 << 20], 2)["ops"]) == 3
