@@ -1,0 +1,410 @@
+"""Benchmark of the GB300 FFT path (prints ONE JSON line on rank 0).
+
+Default workload (the configuration the headline metric is quoted on):
+batched 1D complex FP32 FFTs, n = 4096, batch = 16384 (split re/im, 512 MiB
+per array pair), inputs i.i.d. standard normal from a seed; one step = the
+forward transform of the batch followed by the inverse transform.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--config c2|c1|c3a|c3b|c3c|c4|c5]
+
+value      GFLOP/s by afft's convention (5 N log2 N complex, 2.5 N log2 N
+           real, testing.cpp:1027), inputs resident in HBM, CUDA events on
+           the launching stream, max over ranks.
+e2e        the same metric through the C ABI with pinned HOST buffers: each
+           call stages its input to the device and its result back.
+roofline   the dominant kernel's algorithmic bytes per launch / its mean
+           launch time (CUDA events), against the measured HBM copy peak.
+cpu_baseline  the oracle's FP32 port of afft on the host cores (bounded
+           sample of the same workload).
+--impl reference  times that CPU port alone (all host threads), same metric.
+
+Multi-GPU (torchrun): each rank transforms its own batch (no collective);
+scaling is weak.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+CONFIGS = {
+    # name: (kind, dims, batch, description, inverse_too)
+    "c1": ("c", [1024], 1, "1D c2c n=1024 fwd + inv (latency)", True),
+    "c2": ("c", [4096], 16384, "batched 1D c2c n=4096 x 16384, fwd + inv", True),
+    "c3a": ("c", [256, 256, 256], 1, "3D c2c 256^3 fwd + inv", True),
+    "c3b": ("r", [4096, 4096], 1, "2D r2c 4096^2 + c2r", True),
+    "c3c": ("r", [1 << 20], 64, "64 x 1D r2c n=2^20 + c2r", True),
+    "c4": ("c", [65536], 4096, "batched 1D c2c n=65536 x 4096 fwd", False),
+}
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def flops_of(kind, dims, batch):
+    n = int(np.prod(dims))
+    c = 5.0 if kind in ("c", "ci") else 2.5
+    return c * n * math.log2(n) * batch if n > 1 else 0.0
+
+
+def bytes_of(kind, dims, batch):
+    """Algorithmic bytes of one transform pass: one read + one write."""
+    n = int(np.prod(dims))
+    d = [x for x in dims if x != 1] or [1]
+    h = (d[0] // 2 + 1) * (n // d[0])
+    if kind in ("c", "ci"):
+        return 16 * n * batch
+    return (4 * n + 8 * h) * batch
+
+
+class ClockSampler:
+    """nvidia-smi sampled every 200 ms while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def make_inputs(kind, dims, batch, seed, dev):
+    import torch
+    n = int(np.prod(dims))
+    d = [x for x in dims if x != 1] or [1]
+    h = (d[0] // 2 + 1) * (n // d[0])
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    m = n * batch
+    if kind == "c":
+        a = torch.randn(m, generator=g, device=dev)
+        b = torch.randn(m, generator=g, device=dev)
+        return (a, b), (torch.empty(m, device=dev), torch.empty(m, device=dev)), \
+               (torch.empty(m, device=dev), torch.empty(m, device=dev))
+    # real: x -> half spectrum -> x
+    a = torch.randn(m, generator=g, device=dev)
+    return (a,), (torch.empty(h * batch, device=dev), torch.empty(h * batch, device=dev)), \
+           (torch.empty(m, device=dev),)
+
+
+def cpu_port_rate(kind, dims, batch_total, threads, budget_s):
+    """GFLOP/s of the oracle's FP32 port of afft on `threads` host threads, on
+    a bounded sample of the workload (forward + inverse per transform)."""
+    from oracle import oracle as O
+    n = int(np.prod(dims))
+    fwd = O.Port32(kind, dims)
+    inv = O.Port32("ci" if kind == "c" else "ri", dims)
+    rng = np.random.default_rng(0)
+    # sample size: grow until a pass takes >= budget/4, capped by the workload
+    sample = max(threads, 1)
+    while True:
+        a = rng.standard_normal(fwd.in_elems * sample).astype(np.float32)
+        b = None if kind == "r" else rng.standard_normal(fwd.in_elems * sample).astype(np.float32)
+        t0 = time.perf_counter()
+        out = fwd(a, b, batch=sample, threads=threads)
+        if kind == "c":
+            inv(out[0], out[1], batch=sample, threads=threads)
+        else:
+            inv(out[0], out[1], batch=sample, threads=threads)
+        dt = time.perf_counter() - t0
+        if dt >= budget_s / 4 or sample >= batch_total:
+            break
+        sample = min(batch_total, sample * 4)
+    # timed repeats filling the budget
+    reps = max(1, int(budget_s / max(dt, 1e-6)))
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        out = fwd(a, b, batch=sample, threads=threads)
+        inv(out[0], out[1], batch=sample, threads=threads)
+    dt = time.perf_counter() - t0
+    fl = 2 * flops_of(kind, dims, sample) * reps
+    return fl / dt / 1e9, "%d of %d transforms (fwd+inv) x %d reps, %.1f s" % (sample, batch_total, reps, dt)
+
+
+def run_reference(args, cfg):
+    world, rank, _ = dist_env()
+    kind, dims, batch, desc, _ = CONFIGS[cfg]
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    from oracle import oracle as O
+    O.lib()
+    # bounded: each step is a sample of the workload sized to ~1-3 s
+    rates = []
+    sample_desc = ""
+    for i in range(args.warmup + args.steps):
+        r, sample_desc = cpu_port_rate(kind, dims, batch, threads, budget_s=1.5)
+        if i >= args.warmup:
+            rates.append(r)
+    value = statistics.median(rates)
+    line = {"metric": "GFLOP/s (5N·log2N) & HBM GB/s: TC-split+batched vs plain FP32 at rel-L2≤5e-6",
+            "value": round(value, 3), "unit": "GFLOP/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded standard normal)", "impl": "reference",
+            "config": {"workload": desc},
+            "cpu_baseline": {"value": round(value, 3), "unit": "GFLOP/s", "cores": threads, "kind": "port",
+                             "sample": sample_desc},
+            "e2e": {"value": round(value, 3), "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, cfg):
+    import torch
+    import fft_gb300 as G
+
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local if world > 1 else 0)
+    torch.cuda.set_device(dev)
+    kind, dims, batch, desc, with_inv = CONFIGS[cfg]
+    if args.batch:
+        batch = args.batch
+        desc = desc + " (batch overridden to %d)" % batch
+    fwd = G.BatchPlan(kind, dims, batch)
+    inv = G.BatchPlan("ci" if kind == "c" else "ri", dims, batch) if with_inv else None
+    src, mid, back = make_inputs(kind, dims, batch, 1234 + rank, dev)
+    stream = torch.cuda.Stream(device=dev)   # our kernels and the events share it
+    torch.cuda.synchronize()
+
+    def step():
+        if kind == "c":
+            fwd.launch(src[0], src[1], mid[0], mid[1], stream)
+            if inv:
+                inv.launch(mid[0], mid[1], back[0], back[1], stream)
+        else:
+            fwd.launch(src[0], None, mid[0], mid[1], stream)
+            if inv:
+                inv.launch(mid[0], mid[1], back[0], None, stream)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    barrier()
+    # timed region: events around every launch of the dominant (forward) plan
+    # and around the whole region
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    t_start, t_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev.index) as clk:
+        # untimed soak of the same steps so the 200 ms clock samples cover the
+        # load state of the timed region (which may last only milliseconds)
+        time.sleep(0.3)
+        t_soak = time.perf_counter()
+        while time.perf_counter() - t_soak < args.soak:
+            for _ in range(10):
+                step()
+            torch.cuda.synchronize()
+        barrier()
+        t_start.record(stream)
+        for i in range(args.steps):
+            ev[i][0].record(stream)
+            if kind == "c":
+                fwd.launch(src[0], src[1], mid[0], mid[1], stream)
+            else:
+                fwd.launch(src[0], None, mid[0], mid[1], stream)
+            ev[i][1].record(stream)
+            if inv:
+                if kind == "c":
+                    inv.launch(mid[0], mid[1], back[0], back[1], stream)
+                else:
+                    inv.launch(mid[0], mid[1], back[0], None, stream)
+        t_end.record(stream)
+        barrier()
+    total_ms = t_start.elapsed_time(t_end)
+    fwd_ms = statistics.mean(a.elapsed_time(b) for a, b in ev)
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_step = total_ms / args.steps
+    per_step_flops = flops_of(kind, dims, batch) * (2 if inv else 1)
+    value = per_step_flops * world / (ms_step / 1e3) / 1e9
+    launches_per_step = fwd.launches + (inv.launches if inv else 0)
+
+    # end to end through the C ABI with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        e2e = e2e_rate(args, kind, dims, batch, src, G, torch, world)
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+    hbm, peak_src = peaks()
+    alg_bytes = bytes_of(kind, dims, batch)
+    achieved = alg_bytes / (fwd_ms / 1e3) / 1e9
+    cpu = None
+    if not args.no_cpu:
+        threads = os.cpu_count() or 1
+        rate, sample = cpu_port_rate(kind, dims, batch, threads, budget_s=args.cpu_budget)
+        cpu = {"value": round(rate, 3), "unit": "GFLOP/s", "cores": threads, "kind": "port", "sample": sample}
+    line = {
+        "metric": "GFLOP/s (5N·log2N) & HBM GB/s: TC-split+batched vs plain FP32 at rel-L2≤5e-6",
+        "value": round(value, 2), "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": round(ms_step, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded standard normal)",
+        "config": {"workload": desc, "kind": kind, "dims": dims, "batch_per_gpu": batch,
+                   "form": "plain FP32 Stockham", "l2": "inputs larger than L2 (512 MiB per array pair)"
+                   if bytes_of(kind, dims, batch) > 2 * 129e6 else "working set may fit L2",
+                   "parallelism": "dp%d (independent batches)" % world},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                     "frac": round(achieved / hbm, 4), "traffic": args.traffic, "peak_source": peak_src,
+                     "kernel": "forward plan (%d launch%s), %.4f ms per launch" % (
+                         fwd.launches, "es" if fwd.launches > 1 else "", fwd_ms / fwd.launches)},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": launches_per_step * args.steps,
+        "clocks": dict(clk.summary(), window="soak %.1f s + timed region" % args.soak),
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def e2e_rate(args, kind, dims, batch, src, G, torch, world):
+    """Same metric through the C ABI's synchronous calls with pinned host
+    buffers: every call copies its input to the device and its result back."""
+    fwd = G.BatchPlan(kind, dims, batch)
+    inv = G.BatchPlan("ci" if kind == "c" else "ri", dims, batch)
+    n = int(np.prod(dims))
+    d = [x for x in dims if x != 1] or [1]
+    h = (d[0] // 2 + 1) * (n // d[0])
+    m = n * batch
+    pin = lambda k: torch.empty(k, dtype=torch.float32).pin_memory()
+    if kind == "c":
+        a, b = pin(m), pin(m)
+        a.copy_(src[0].cpu())
+        b.copy_(src[1].cpu())
+        o1, o2, r1, r2 = pin(m), pin(m), pin(m), pin(m)
+
+        def step():
+            fwd(a, b, o1, o2)
+            inv(o1, o2, r1, r2)
+        h2d = 2 * (2 * m * 4)
+        d2h = 2 * (2 * m * 4)
+    else:
+        a = pin(m)
+        a.copy_(src[0].cpu())
+        o1, o2, r1 = pin(h * batch), pin(h * batch), pin(m)
+
+        def step():
+            fwd(a, o1, o2)
+            inv(o1, o2, r1)
+        h2d = 4 * m + 8 * h * batch
+        d2h = 8 * h * batch + 4 * m
+    steps = max(2, min(args.steps, 5))
+    step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    dt = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([dt], device=torch.device("cuda", torch.cuda.current_device()))
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dt = float(t.item())
+    val = 2 * flops_of(kind, dims, batch) * world * steps / dt / 1e9
+    return {"value": round(val, 2), "unit": "GFLOP/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+            "steps": steps}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
+    ap.add_argument("--batch", type=int, default=0, help="override the batch (profiling a smaller case)")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=10.0)
+    ap.add_argument("--soak", type=float, default=1.5, help="seconds of untimed load before the timed region")
+    ap.add_argument("--traffic", type=float, default=None,
+                    help="ncu dram bytes per launch of the dominant kernel, if measured")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args, args.config)
+    else:
+        run_ours(args, args.config)
+
+
+if __name__ == "__main__":
+    main()

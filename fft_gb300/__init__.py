@@ -256,7 +256,7 @@ class BatchPlan:
 
     def launch(self, src_re, src_im, dst_re, dst_im, stream=None):
         """Enqueue without waiting; ``stream`` is a torch.cuda.Stream, a raw
-        cudaStream_t int, or None for the plan's own stream."""
+        cudaStream_t int, or None for the CUDA default stream."""
         s = stream.cuda_stream if hasattr(stream, "cuda_stream") else stream
         rc = lib().afft_gb300_transform_async(self.state, ptr(src_re), ptr(src_im), ptr(dst_re), ptr(dst_im), s)
         if rc:

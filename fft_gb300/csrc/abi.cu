@@ -345,8 +345,8 @@ int afft_gb300_transform_async(void* plan, const float* sr, const float* si, flo
   if (!P) return AFFT_GB300_ESTATE;
   std::lock_guard<std::mutex> g(P->mu);
   cudaSetDevice(P->device);
-  cudaStream_t st = stream ? (cudaStream_t)stream : P->stream;
-  return P->launch(sr, si, dr, di, st);
+  // NULL is the CUDA default stream, as for a kernel launch
+  return P->launch(sr, si, dr, di, (cudaStream_t)stream);
 }
 
 int afft_gb300_release(void* plan) {

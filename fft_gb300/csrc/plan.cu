@@ -220,6 +220,13 @@ struct Builder {
     op.p.tw_qmask = tw_qmask;
     op.p.tw_qshift = tw_qshift;
     if (!dry) {
+      if (op.k.smem > 48 * 1024 &&
+          cudaFuncSetAttribute((const void*)op.k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)op.k.smem) != cudaSuccess) {
+        cudaGetLastError();
+        fail("kernel shared memory configuration failed");
+        return;
+      }
       op.p.tw = stage_twiddles(logl);
       if (tw_n) fourstep_tables(tw_n, &op.p.tw_hi, &op.p.tw_lo, &op.p.tw_lo_bits);
       if (real_L) op.p.rtw = real_twiddles(real_L);
@@ -571,9 +578,6 @@ int Plan::launch(const float* src_re, const float* src_im, float* dst_re, float*
       LineParams p = op.p;
       p.in = bind(op.in, base);
       p.out = bind(op.out, base);
-      if (op.smem > 48 * 1024) {
-        cudaFuncSetAttribute((const void*)op.k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)op.smem);
-      }
       op.k.fn<<<(unsigned)op.grid, op.threads, op.smem, st>>>(p);
     } else if (op.type == OP_REAL) {
       RealPassParams rp = op.rp;

@@ -91,7 +91,7 @@ int afft_gb300_queue_run(afft_gb300_queue* q, void* stream) {
   }
   QueueImpl& Q = q->impl;
   cudaSetDevice(Q.device);
-  cudaStream_t st = stream ? (cudaStream_t)stream : Q.stream;
+  cudaStream_t st = (cudaStream_t)stream;
   if (!Q.exec) {
     // scratch must exist before capture
     for (auto& kv : Q.plans) {

@@ -179,9 +179,10 @@ AFFT_GB300_API void* afft_gb300_batch_create(int kind, size_t ndim, const size_t
   size_t batch, int format, void* mem);
 
 /* Enqueue one transform of `plan` (any kind; real forward ignores src_im,
- * real inverse ignores dst_im) on `stream` (a cudaStream_t; NULL = the
- * plan's own stream) without waiting for it.  All four data pointers must be
- * device-accessible.  Returns 0 or an AFFT_GB300_* code. */
+ * real inverse ignores dst_im) on `stream` (a cudaStream_t; NULL = the CUDA
+ * default stream, as for a kernel launch) without waiting for it.  All four
+ * data pointers must be device-accessible.  Returns 0 or an AFFT_GB300_*
+ * code. */
 AFFT_GB300_API int afft_gb300_transform_async(void* plan, const float* src_re,
   const float* src_im, float* dst_re, float* dst_im, void* stream);
 
@@ -221,6 +222,7 @@ typedef struct afft_gb300_desc
 typedef struct afft_gb300_queue afft_gb300_queue;
 AFFT_GB300_API afft_gb300_queue* afft_gb300_queue_create(const afft_gb300_desc* descs,
   size_t count);
+/* `stream` as for afft_gb300_transform_async (NULL = default stream). */
 AFFT_GB300_API int afft_gb300_queue_run(afft_gb300_queue* q, void* stream);
 /* Kernel launches one run issues (after grouping). */
 AFFT_GB300_API int afft_gb300_queue_launches(const afft_gb300_queue* q);
