@@ -194,7 +194,9 @@ static int transform_sync(void* plan, const float* sr, const float* si, float* d
     }
     return 0;
   }
-  // host data: stage through plan-owned device buffers
+  // host data: stage through plan-owned device buffers.  A batch is cut
+  // into chunks so the copy of chunk i+1 in, the transform of chunk i and the
+  // copy of chunk i-1 out overlap (three streams, ordered by events).
   long long in_n, out_n;
   io_elems(*P, &in_n, &out_n);
   size_t fin = (size_t)in_n * (inter && !real_in ? 2 : 1);   // floats of src_re
@@ -215,14 +217,47 @@ static int transform_sync(void* plan, const float* sr, const float* si, float* d
   float* d_si = use_si ? d_sr + fin : nullptr;
   float* d_dr = d_sr + fin + (use_si ? fin : 0);
   float* d_di = use_di ? d_dr + fout : nullptr;
-  cudaStream_t st = P->stream;
-  cudaMemcpyAsync(d_sr, sr, fin * sizeof(float), cudaMemcpyDefault, st);
-  if (use_si) cudaMemcpyAsync(d_si, si, fin * sizeof(float), cudaMemcpyDefault, st);
-  int rc = P->launch(d_sr, d_si, d_dr, d_di, st);
-  if (rc) return rc;
-  cudaMemcpyAsync(dr, d_dr, fout * sizeof(float), cudaMemcpyDefault, st);
-  if (use_di) cudaMemcpyAsync(di, d_di, fout * sizeof(float), cudaMemcpyDefault, st);
-  cudaError_t e = cudaStreamSynchronize(st);
+  if (!P->copy_in) {
+    // chunking: the largest divisor of the batch up to 8, for batches whose
+    // data is worth overlapping (>= 8 MiB)
+    long long k = 1;
+    if (need >= (8u << 20))
+      for (long long d = 8; d >= 2; d--)
+        if (P->batch % d == 0) { k = d; break; }
+    if (k > 1) {
+      P->chunk = build_plan(P->kind, P->ndim, P->dims, P->batch / k, P->format);
+      if (!P->chunk) k = 1;
+    }
+    P->nchunks = k;
+    if (cudaStreamCreateWithFlags(&P->copy_in, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&P->copy_out, cudaStreamNonBlocking) != cudaSuccess) {
+      cudaGetLastError();
+      set_error(AFFT_GB300_ECUDA, "stream creation failed");
+      return AFFT_GB300_ECUDA;
+    }
+    P->ev.resize(2 * k);
+    for (auto& e : P->ev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+  }
+  const long long k = P->nchunks;
+  const size_t cin = fin / k, cout = fout / k;    // floats per chunk, per array
+  for (long long i = 0; i < k; i++) {
+    cudaMemcpyAsync(d_sr + i * cin, sr + i * cin, cin * sizeof(float), cudaMemcpyDefault, P->copy_in);
+    if (use_si) cudaMemcpyAsync(d_si + i * cin, si + i * cin, cin * sizeof(float), cudaMemcpyDefault, P->copy_in);
+    cudaEventRecord(P->ev[2 * i], P->copy_in);
+  }
+  Plan& C = k > 1 ? *P->chunk : *P;
+  for (long long i = 0; i < k; i++) {
+    cudaStreamWaitEvent(P->stream, P->ev[2 * i], 0);
+    int rc = C.launch(d_sr + i * cin, use_si ? d_si + i * cin : nullptr, d_dr + i * cout,
+                      use_di ? d_di + i * cout : nullptr, P->stream);
+    if (rc) return rc;
+    cudaEventRecord(P->ev[2 * i + 1], P->stream);
+    cudaStreamWaitEvent(P->copy_out, P->ev[2 * i + 1], 0);
+    cudaMemcpyAsync(dr + i * cout, d_dr + i * cout, cout * sizeof(float), cudaMemcpyDefault, P->copy_out);
+    if (use_di) cudaMemcpyAsync(di + i * cout, d_di + i * cout, cout * sizeof(float), cudaMemcpyDefault, P->copy_out);
+  }
+  cudaError_t e = cudaStreamSynchronize(P->copy_out);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(P->stream);
   if (e != cudaSuccess) {
     set_error(AFFT_GB300_ECUDA, cudaGetErrorString(e));
     return AFFT_GB300_ECUDA;

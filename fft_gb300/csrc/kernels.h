@@ -50,7 +50,7 @@ LineKernel make_line_kernel() {
   k.tstore = TSTORE;
   k.lines_per_cta = C;
   k.threads = Sched<LOGL>::T * C;
-  k.smem = (size_t)2 * C * L * sizeof(float);
+  k.smem = (size_t)Smem<L, C, COLS>::FLOAT2S * sizeof(float2);
   return k;
 }
 

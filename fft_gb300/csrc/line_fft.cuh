@@ -177,31 +177,24 @@ __device__ __forceinline__ void dft(float2 (&x)[R]) {
 }
 
 // ---------------------------------------------------------------------------
-// shared-memory layouts (split re/im float arrays)
+// shared-memory layout: complex values as float2, padded so the Stockham
+// scatter and the canonical gather hit distinct bank pairs per half-warp and
+// every per-element offset is a compile-time constant:
+//   rows mode: line c at c * LP, element j at j + j/16   (LP = L + L/16)
+//   cols mode: element j of line c at j * CP + c          (CP = C + 1)
 // ---------------------------------------------------------------------------
 template <int L, int C, bool COLS>
 struct Smem {
-  float* re;
-  float* im;
+  static constexpr int LP = L + L / 16;
+  static constexpr int CP = C + 1;
+  static constexpr int FLOAT2S = COLS ? L * CP : C * LP;
+  float2* s;
   __device__ __forceinline__ int idx(int c, int j) const {
-    if constexpr (COLS) {
-      constexpr int LC = C >= 32 ? 5 : (C >= 16 ? 4 : (C >= 8 ? 3 : (C >= 4 ? 2 : (C >= 2 ? 1 : 0))));
-      if constexpr (C == 1) return j;
-      else return j * C + (c ^ ((j >> (5 - LC)) & (C - 1)));
-    } else {
-      int f = c * L + j;
-      return f ^ (((f >> 5) & 15) | ((f >> 4) & 16)) ^ ((f >> 9) & 31);
-    }
+    if constexpr (COLS) return j * CP + c;
+    else return c * LP + j + (j >> 4);
   }
-  __device__ __forceinline__ void put(int c, int j, float2 v) const {
-    int k = idx(c, j);
-    re[k] = v.x;
-    im[k] = v.y;
-  }
-  __device__ __forceinline__ float2 get(int c, int j) const {
-    int k = idx(c, j);
-    return make_float2(re[k], im[k]);
-  }
+  __device__ __forceinline__ void put(int c, int j, float2 v) const { s[idx(c, j)] = v; }
+  __device__ __forceinline__ float2 get(int c, int j) const { return s[idx(c, j)]; }
 };
 
 template <bool WARP_ONLY>
@@ -285,15 +278,26 @@ __device__ __forceinline__ float2 fourstep_twiddle(const LineParams& p, long lon
 // ---------------------------------------------------------------------------
 // the kernel
 // ---------------------------------------------------------------------------
+// Register budget per thread: with 64 the allocator keeps 4 CTAs of 256
+// threads resident per SM, which measured faster at every length than the
+// unconstrained (~80 register) build.
+#ifndef AFFT_REG_CAP
+#define AFFT_REG_CAP 64
+#endif
+template <int NT>
+constexpr int min_ctas() {
+  return AFFT_REG_CAP ? (65536 / (AFFT_REG_CAP * NT) > 0 ? 65536 / (AFFT_REG_CAP * NT) : 1) : 1;
+}
+
 template <int LOGL, int C, bool COLS, int KIND, bool TSTORE>
-__global__ void __launch_bounds__(Sched<LOGL>::T * C)
+__global__ void __launch_bounds__(Sched<LOGL>::T * C, min_ctas<Sched<LOGL>::T * C>())
 line_fft(const LineParams p) {
   using Sc = Sched<LOGL>;
   constexpr int L = Sc::L, E = Sc::E, T = Sc::T;
   // a line lives inside one warp: rows mode with T <= 32, or a single line
   constexpr bool WARP_ONLY = (!COLS && T <= 32) || (T * C <= 32);
-  extern __shared__ float smem_raw[];
-  Smem<L, C, COLS> sm{smem_raw, smem_raw + C * L};
+  extern __shared__ float2 smem_raw[];
+  Smem<L, C, COLS> sm{smem_raw};
 
   const int tid = threadIdx.x;
   const int c = COLS ? (tid % C) : (tid / T);

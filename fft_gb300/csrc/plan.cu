@@ -548,6 +548,9 @@ Plan::~Plan() {
   if (scratch) cudaFree(scratch);
   if (stage) cudaFree(stage);
   if (stream) cudaStreamDestroy(stream);
+  if (copy_in) cudaStreamDestroy(copy_in);
+  if (copy_out) cudaStreamDestroy(copy_out);
+  for (auto e : ev) cudaEventDestroy(e);
 }
 
 static inline float* resolve(const Ref& r, float* const* base) { return base[r.buf] ? base[r.buf] + r.off : nullptr; }

@@ -68,6 +68,12 @@ struct Plan {
   // device staging for host-resident data
   float* stage = nullptr;
   size_t stage_bytes = 0;
+  // host-data pipeline: a plan for a chunk of the batch, so copies of one
+  // chunk overlap the transform of the previous one
+  std::unique_ptr<Plan> chunk;
+  long long nchunks = 1;
+  cudaStream_t copy_in = nullptr, copy_out = nullptr;
+  std::vector<cudaEvent_t> ev;
   std::mutex mu;
 
   ~Plan();

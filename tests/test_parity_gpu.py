@@ -318,3 +318,40 @@ def test_queue_mixed(dev):
         for (kind, dims, a, b), it in zip(host, items):
             got = it[4].cpu().numpy() if kind == "ri" else (it[4].cpu().numpy(), it[5].cpu().numpy())
             check(kind, dims, a, b, got)
+
+
+@pytest.mark.parametrize("kind", ["c", "ci", "r", "ri"])
+def test_batch_host_pointers_pipelined(kind, dev):
+    # host data large enough that the library cuts the batch into chunks and
+    # overlaps copies with transforms
+    dims, batch = [4096], 512
+    n = 4096
+    h = n // 2 + 1
+    in_n = {"c": n, "ci": n, "r": n, "ri": h}[kind]
+    out_n = {"c": n, "ci": n, "r": h, "ri": n}[kind]
+    rng = np.random.default_rng(21)
+    a = rng.standard_normal(in_n * batch).astype(np.float32)
+    b = None if kind == "r" else rng.standard_normal(in_n * batch).astype(np.float32)
+    pin = lambda m: torch.zeros(m, dtype=torch.float32).pin_memory()
+    pa = pin(a.size)
+    pa.copy_(torch.from_numpy(a))
+    pb = None
+    if b is not None:
+        pb = pin(b.size)
+        pb.copy_(torch.from_numpy(b))
+    oa = pin(out_n * batch)
+    ob = None if kind == "ri" else pin(out_n * batch)
+    plan = G.BatchPlan(kind, dims, batch)
+    for _ in range(2):
+        if kind in ("c", "ci"):
+            plan(pa, pb, oa, ob)
+        elif kind == "r":
+            plan(pa, oa, ob)
+        else:
+            plan(pa, pb, oa)
+    oa_n = oa.numpy()
+    ob_n = None if ob is None else ob.numpy()
+    for j in (0, 1, 255, 511):
+        si, so = slice(j * in_n, (j + 1) * in_n), slice(j * out_n, (j + 1) * out_n)
+        got = oa_n[so] if kind == "ri" else (oa_n[so], ob_n[so])
+        check(kind, dims, a[si], None if b is None else b[si], got)
