@@ -6,9 +6,11 @@
 namespace agb {
 
 typedef void (*LineKernelFn)(LineParams);
+typedef void (*GroupedKernelFn)(const Segment*, int, long long);
 
 struct LineKernel {
   LineKernelFn fn;
+  GroupedKernelFn grouped;
   int logl;
   int cols;            // thread mapping: 1 = across lines, 0 = along a line
   int kind;            // LK_C2C / LK_R2C / LK_C2R
@@ -44,6 +46,7 @@ LineKernel make_line_kernel() {
   constexpr int L = 1 << LOGL;
   LineKernel k;
   k.fn = &line_fft<LOGL, C, COLS, KIND, TSTORE>;
+  k.grouped = &line_fft_grouped<LOGL, C, COLS, KIND, TSTORE>;
   k.logl = LOGL;
   k.cols = COLS;
   k.kind = KIND;

@@ -289,9 +289,9 @@ constexpr int min_ctas() {
   return AFFT_REG_CAP ? (65536 / (AFFT_REG_CAP * NT) > 0 ? 65536 / (AFFT_REG_CAP * NT) : 1) : 1;
 }
 
+// The body of one CTA's work: lines [cta*C, cta*C + C) of the launch `p`.
 template <int LOGL, int C, bool COLS, int KIND, bool TSTORE>
-__global__ void __launch_bounds__(Sched<LOGL>::T * C, min_ctas<Sched<LOGL>::T * C>())
-line_fft(const LineParams p) {
+__device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta) {
   using Sc = Sched<LOGL>;
   constexpr int L = Sc::L, E = Sc::E, T = Sc::T;
   // a line lives inside one warp: rows mode with T <= 32, or a single line
@@ -302,7 +302,7 @@ line_fft(const LineParams p) {
   const int tid = threadIdx.x;
   const int c = COLS ? (tid % C) : (tid / T);
   const int t = COLS ? (tid / C) : (tid % T);
-  const long long q = (long long)blockIdx.x * C + c;
+  const long long q = cta * C + c;
   const bool active = q < p.nlines;
 
   float2 v[E];
@@ -371,7 +371,7 @@ line_fft(const LineParams p) {
       for (int e = 0; e < E; e++) sm.put(c, t + T * e, v[e]);
       __syncthreads();
       const int c2 = tid / T, t2 = tid % T;
-      const long long q2 = (long long)blockIdx.x * C + c2;
+      const long long q2 = cta * C + c2;
       if (q2 < p.nlines) {
         const long long base = line_off(p.out, q2);
 #pragma unroll
@@ -438,6 +438,40 @@ line_fft(const LineParams p) {
   }
 }
 
+template <int LOGL, int C, bool COLS, int KIND, bool TSTORE>
+__global__ void __launch_bounds__(Sched<LOGL>::T * C, min_ctas<Sched<LOGL>::T * C>())
+line_fft(const LineParams p) {
+  line_fft_body<LOGL, C, COLS, KIND, TSTORE>(p, blockIdx.x);
+}
+
+// One launch of a multi-transform queue: a device-side table of segments
+// (one per transform pass of this kernel shape), each covering `nctas`
+// virtual CTAs starting at cta0 (ascending).  Persistent: every CTA walks the
+// virtual CTA range with a grid stride, finds its segment by binary search,
+// stages the segment's parameters in shared memory and runs the body.
+struct Segment {
+  LineParams p;
+  long long cta0;
+};
+
+template <int LOGL, int C, bool COLS, int KIND, bool TSTORE>
+__global__ void __launch_bounds__(Sched<LOGL>::T * C, min_ctas<Sched<LOGL>::T * C>())
+line_fft_grouped(const Segment* __restrict__ segs, int nseg, long long total) {
+  __shared__ LineParams sp;
+  for (long long v = blockIdx.x; v < total; v += gridDim.x) {
+    int lo = 0, hi = nseg - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (segs[mid].cta0 <= v) lo = mid;
+      else hi = mid - 1;
+    }
+    __syncthreads();   // previous iteration done with sp and the staging buffers
+    if (threadIdx.x == 0) sp = segs[lo].p;
+    __syncthreads();
+    line_fft_body<LOGL, C, COLS, KIND, TSTORE>(sp, v - segs[lo].cta0);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // standalone real pre/post pass for transforms too long for one CTA
 // ---------------------------------------------------------------------------
@@ -461,6 +495,18 @@ struct CopyParams {
   long long nlines, len;
 };
 __global__ void copy_lines_kernel(const CopyParams p);
+
+// Elementwise ops of a multi-transform queue (real pass, copy, size-1 real)
+// in one persistent launch over a segment table, as for line_fft_grouped;
+// every segment covers `nblocks` virtual blocks of 256 threads.
+enum { EW_REAL = 0, EW_COPY = 1, EW_REAL1 = 2 };
+struct EwSegment {
+  int type;
+  RealPassParams rp;
+  CopyParams cp;
+  long long blk0;
+};
+__global__ void elementwise_grouped(const EwSegment* __restrict__ segs, int nseg, long long total);
 
 // Real transforms of total size 1: X[0] = x[0] + 0i (forward), x[0] = re X[0]
 // (inverse), one element per line.

@@ -1,9 +1,21 @@
-// Multi-transform queue (afft_gb300_queue_*): many transforms of mixed
-// sizes and kinds run as one unit.  Plans are built once per distinct
-// (kind, shape); the launches of every transform are recorded into one CUDA
-// graph on the first run and replayed afterwards.
+// Multi-transform queue (afft_gb300_queue_*): many transforms of mixed sizes
+// and kinds in one unit of work.
+//
+// At creation every transform's plan (one per distinct kind and shape) is
+// resolved against the transform's own pointers into concrete launch
+// segments: pass i of a transform becomes a segment of "level" i.  Segments
+// are grouped by (level, kernel shape) into device-side descriptor tables;
+// each group is ONE persistent launch (line_fft_grouped or
+// elementwise_grouped) whose CTAs walk the table.  Groups of one level are
+// independent and become parallel branches of a CUDA graph; levels follow
+// each other.  The first run captures the graph, later runs replay it.
+//
+// Scratch for transforms whose plans need it (four-step passes, real
+// inverse of N-D arrays) comes from one queue-owned arena, a disjoint region
+// per transform.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <map>
 #include <tuple>
 #include <vector>
@@ -13,19 +25,236 @@
 
 namespace agb {
 
+struct Group {
+  int level = 0;
+  bool line = true;
+  LineKernel k{};
+  std::vector<Segment> segs;
+  std::vector<EwSegment> esegs;
+  long long total = 0;   // virtual CTAs / blocks
+  void* d_tab = nullptr;
+  int grid = 0, threads = 0;
+  size_t smem = 0;
+};
+
 struct QueueImpl {
   std::vector<afft_gb300_desc> descs;
-  std::vector<std::shared_ptr<Plan>> plan_of;   // per descriptor
   std::map<std::vector<long long>, std::shared_ptr<Plan>> plans;
+  std::vector<Group> groups;
+  float* arena = nullptr;
   cudaGraphExec_t exec = nullptr;
   cudaStream_t stream = nullptr;
-  int launches = 0;
+  std::vector<cudaStream_t> pool;
+  std::vector<cudaEvent_t> events;
   int device = 0;
   ~QueueImpl() {
     if (exec) cudaGraphExecDestroy(exec);
+    for (auto& g : groups)
+      if (g.d_tab) cudaFree(g.d_tab);
+    if (arena) cudaFree(arena);
+    for (auto s : pool) cudaStreamDestroy(s);
+    for (auto e : events) cudaEventDestroy(e);
     if (stream) cudaStreamDestroy(stream);
   }
 };
+
+static LineIO bind_io(const IOSpec& s, float* const* base) {
+  LineIO o;
+  o.re = base[s.re.buf] ? base[s.re.buf] + s.re.off : nullptr;
+  o.im = base[s.im.buf] ? base[s.im.buf] + s.im.off : nullptr;
+  o.es = s.es;
+  o.lo = s.lo;
+  o.hi = s.hi;
+  o.qshift = s.qshift;
+  o.qmask = s.qmask;
+  return o;
+}
+
+static int build_queue(QueueImpl& Q) {
+  int nsm = 0;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, Q.device);
+  // plans and scratch layout
+  std::vector<std::shared_ptr<Plan>> plan_of;
+  std::vector<long long> scr_off;
+  long long arena_floats = 0;
+  for (const auto& d : Q.descs) {
+    int nd;
+    long long dims[64];
+    if (d.kind < 0 || d.kind > 3 || d.ndim < 1 || d.ndim > 3 || validate_shape(d.ndim, d.dim, &nd, dims)) {
+      set_error(AFFT_GB300_EINVAL, "bad descriptor (kind, ndim 1..3, power-of-two dims)");
+      return AFFT_GB300_EINVAL;
+    }
+    std::vector<long long> key{d.kind};
+    key.insert(key.end(), dims, dims + nd);
+    auto it = Q.plans.find(key);
+    if (it == Q.plans.end()) {
+      auto P = build_plan(d.kind, nd, dims, 1, 0);
+      if (!P) return AFFT_GB300_EINVAL;
+      it = Q.plans.emplace(key, std::shared_ptr<Plan>(P.release())).first;
+    }
+    plan_of.push_back(it->second);
+    scr_off.push_back(arena_floats);
+    arena_floats += (it->second->scratch_floats + 63) / 64 * 64;
+  }
+  if (arena_floats && cudaMalloc(&Q.arena, (size_t)arena_floats * sizeof(float)) != cudaSuccess) {
+    cudaGetLastError();
+    set_error(AFFT_GB300_ENOMEM, "queue scratch allocation failed");
+    return AFFT_GB300_ENOMEM;
+  }
+  // segments, grouped by (level, kernel)
+  std::map<std::pair<int, const void*>, size_t> gidx;
+  for (size_t j = 0; j < Q.descs.size(); j++) {
+    const auto& d = Q.descs[j];
+    float* base[B_NBUF] = {(float*)d.src_re, (float*)d.src_im, d.dst_re, d.dst_im,
+                           Q.arena ? Q.arena + scr_off[j] : nullptr};
+    const Plan& P = *plan_of[j];
+    for (size_t i = 0; i < P.ops.size(); i++) {
+      const Op& op = P.ops[i];
+      const void* kid = op.type == OP_LINE ? (const void*)op.k.grouped : (const void*)&elementwise_grouped;
+      auto key = std::make_pair((int)i, kid);
+      auto it = gidx.find(key);
+      if (it == gidx.end()) {
+        Group g;
+        g.level = (int)i;
+        g.line = op.type == OP_LINE;
+        g.k = op.k;
+        it = gidx.emplace(key, Q.groups.size()).first;
+        Q.groups.push_back(g);
+      }
+      Group& g = Q.groups[it->second];
+      if (op.type == OP_LINE) {
+        Segment s;
+        s.p = op.p;
+        s.p.in = bind_io(op.in, base);
+        s.p.out = bind_io(op.out, base);
+        s.cta0 = op.grid;  // for now the segment's CTA count
+        g.segs.push_back(s);
+      } else {
+        EwSegment s{};
+        s.type = op.type == OP_REAL ? EW_REAL : (op.type == OP_COPY ? EW_COPY : EW_REAL1);
+        s.rp = op.rp;
+        s.cp = op.cp;
+        if (op.type == OP_COPY) {
+          s.cp.in = bind_io(op.in, base);
+          s.cp.out = bind_io(op.out, base);
+        } else {
+          s.rp.in = bind_io(op.in, base);
+          s.rp.out = bind_io(op.out, base);
+        }
+        s.blk0 = op.grid;
+        g.esegs.push_back(s);
+      }
+    }
+  }
+  // largest segments first, prefix sums, device tables, launch shapes
+  for (auto& g : Q.groups) {
+    void* host = nullptr;
+    size_t bytes = 0;
+    if (g.line) {
+      std::stable_sort(g.segs.begin(), g.segs.end(),
+                       [](const Segment& a, const Segment& b) { return a.cta0 > b.cta0; });
+      long long acc = 0;
+      for (auto& s : g.segs) {
+        long long n = s.cta0;
+        s.cta0 = acc;
+        acc += n;
+      }
+      g.total = acc;
+      host = g.segs.data();
+      bytes = g.segs.size() * sizeof(Segment);
+      g.threads = g.k.threads;
+      g.smem = g.k.smem;
+      if (g.smem > 48 * 1024 &&
+          cudaFuncSetAttribute((const void*)g.k.grouped, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)g.smem) != cudaSuccess) {
+        cudaGetLastError();
+        set_error(AFFT_GB300_ECUDA, "kernel shared memory configuration failed");
+        return AFFT_GB300_ECUDA;
+      }
+      int per_sm = 1;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, g.k.grouped, g.threads, g.smem);
+      g.grid = (int)std::min<long long>(g.total, (long long)std::max(per_sm, 1) * nsm);
+    } else {
+      std::stable_sort(g.esegs.begin(), g.esegs.end(),
+                       [](const EwSegment& a, const EwSegment& b) { return a.blk0 > b.blk0; });
+      long long acc = 0;
+      for (auto& s : g.esegs) {
+        long long n = s.blk0;
+        s.blk0 = acc;
+        acc += n;
+      }
+      g.total = acc;
+      host = g.esegs.data();
+      bytes = g.esegs.size() * sizeof(EwSegment);
+      g.threads = 256;
+      g.grid = (int)std::min<long long>(g.total, 8LL * nsm);
+    }
+    if (cudaMalloc(&g.d_tab, bytes) != cudaSuccess ||
+        cudaMemcpy(g.d_tab, host, bytes, cudaMemcpyHostToDevice) != cudaSuccess) {
+      cudaGetLastError();
+      set_error(AFFT_GB300_ENOMEM, "queue descriptor upload failed");
+      return AFFT_GB300_ENOMEM;
+    }
+  }
+  std::stable_sort(Q.groups.begin(), Q.groups.end(), [](const Group& a, const Group& b) {
+    return a.level != b.level ? a.level < b.level : a.total > b.total;
+  });
+  return 0;
+}
+
+static void launch_group(const Group& g, cudaStream_t st) {
+  if (g.total == 0) return;
+  if (g.line)
+    g.k.grouped<<<g.grid, g.threads, g.smem, st>>>((const Segment*)g.d_tab, (int)g.segs.size(), g.total);
+  else
+    elementwise_grouped<<<g.grid, g.threads, 0, st>>>((const EwSegment*)g.d_tab, (int)g.esegs.size(), g.total);
+}
+
+static int capture(QueueImpl& Q) {
+  size_t width = 1;
+  for (size_t i = 0; i < Q.groups.size();) {
+    size_t j = i;
+    while (j < Q.groups.size() && Q.groups[j].level == Q.groups[i].level) j++;
+    width = std::max(width, j - i);
+    i = j;
+  }
+  width = std::min<size_t>(width, 16);
+  while (Q.pool.size() < width) {
+    cudaStream_t s;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return AFFT_GB300_ECUDA;
+    Q.pool.push_back(s);
+  }
+  while (Q.events.size() < Q.groups.size() + 1) {
+    cudaEvent_t e;
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return AFFT_GB300_ECUDA;
+    Q.events.push_back(e);
+  }
+  cudaStream_t s0 = Q.stream;
+  if (cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return AFFT_GB300_ECUDA;
+  for (size_t i = 0; i < Q.groups.size();) {
+    size_t j = i;
+    while (j < Q.groups.size() && Q.groups[j].level == Q.groups[i].level) j++;
+    if (j - i == 1) {
+      launch_group(Q.groups[i], s0);
+    } else {
+      cudaEventRecord(Q.events.back(), s0);   // fork
+      for (size_t g = i; g < j; g++) {
+        cudaStream_t sg = Q.pool[(g - i) % Q.pool.size()];
+        cudaStreamWaitEvent(sg, Q.events.back(), 0);
+        launch_group(Q.groups[g], sg);
+        cudaEventRecord(Q.events[g], sg);
+      }
+      for (size_t g = i; g < j; g++) cudaStreamWaitEvent(s0, Q.events[g], 0);   // join
+    }
+    i = j;
+  }
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamEndCapture(s0, &graph);
+  if (e != cudaSuccess) return AFFT_GB300_ECUDA;
+  e = cudaGraphInstantiate(&Q.exec, graph, 0);
+  cudaGraphDestroy(graph);
+  return e == cudaSuccess ? 0 : AFFT_GB300_ECUDA;
+}
 
 }  // namespace agb
 
@@ -47,36 +276,13 @@ afft_gb300_queue* afft_gb300_queue_create(const afft_gb300_desc* descs, size_t c
   QueueImpl& Q = q->impl;
   cudaGetDevice(&Q.device);
   Q.descs.assign(descs, descs + count);
-  for (const auto& d : Q.descs) {
-    if (d.kind < 0 || d.kind > 3 || d.ndim < 1 || d.ndim > 3) {
-      set_error(AFFT_GB300_EINVAL, "bad descriptor");
-      delete q;
-      return nullptr;
-    }
-    int nd;
-    long long dims[64];
-    if (validate_shape(d.ndim, d.dim, &nd, dims)) {
-      set_error(AFFT_GB300_EINVAL, "descriptor dimensions must be powers of two");
-      delete q;
-      return nullptr;
-    }
-    std::vector<long long> key{d.kind};
-    key.insert(key.end(), dims, dims + nd);
-    auto it = Q.plans.find(key);
-    if (it == Q.plans.end()) {
-      auto P = build_plan(d.kind, nd, dims, 1, 0);
-      if (!P) {
-        delete q;
-        return nullptr;
-      }
-      it = Q.plans.emplace(key, std::shared_ptr<Plan>(P.release())).first;
-    }
-    Q.plan_of.push_back(it->second);
-    Q.launches += (int)it->second->ops.size();
-  }
   if (cudaStreamCreateWithFlags(&Q.stream, cudaStreamNonBlocking) != cudaSuccess) {
     cudaGetLastError();
     set_error(AFFT_GB300_ECUDA, "stream creation failed");
+    delete q;
+    return nullptr;
+  }
+  if (build_queue(Q)) {
     delete q;
     return nullptr;
   }
@@ -91,43 +297,12 @@ int afft_gb300_queue_run(afft_gb300_queue* q, void* stream) {
   }
   QueueImpl& Q = q->impl;
   cudaSetDevice(Q.device);
-  cudaStream_t st = (cudaStream_t)stream;
-  if (!Q.exec) {
-    // scratch must exist before capture
-    for (auto& kv : Q.plans) {
-      Plan& P = *kv.second;
-      if (P.scratch_floats > 0 && !P.scratch &&
-          cudaMalloc(&P.scratch, (size_t)P.scratch_floats * sizeof(float)) != cudaSuccess) {
-        cudaGetLastError();
-        set_error(AFFT_GB300_ENOMEM, "scratch allocation failed");
-        return AFFT_GB300_ENOMEM;
-      }
-    }
-    cudaStream_t cap = Q.stream;
-    if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
-      set_error(AFFT_GB300_ECUDA, "graph capture failed");
-      return AFFT_GB300_ECUDA;
-    }
-    int rc = 0;
-    for (size_t i = 0; i < Q.descs.size() && !rc; i++) {
-      const auto& d = Q.descs[i];
-      rc = Q.plan_of[i]->launch(d.src_re, d.src_im, d.dst_re, d.dst_im, cap);
-    }
-    cudaGraph_t g = nullptr;
-    cudaError_t e = cudaStreamEndCapture(cap, &g);
-    if (rc || e != cudaSuccess) {
-      if (g) cudaGraphDestroy(g);
-      set_error(AFFT_GB300_ECUDA, "graph capture failed");
-      return AFFT_GB300_ECUDA;
-    }
-    e = cudaGraphInstantiate(&Q.exec, g, 0);
-    cudaGraphDestroy(g);
-    if (e != cudaSuccess) {
-      set_error(AFFT_GB300_ECUDA, cudaGetErrorString(e));
-      return AFFT_GB300_ECUDA;
-    }
+  if (!Q.exec && capture(Q)) {
+    cudaGetLastError();
+    set_error(AFFT_GB300_ECUDA, "graph capture failed");
+    return AFFT_GB300_ECUDA;
   }
-  cudaError_t e = cudaGraphLaunch(Q.exec, st);
+  cudaError_t e = cudaGraphLaunch(Q.exec, (cudaStream_t)stream);
   if (e != cudaSuccess) {
     set_error(AFFT_GB300_ECUDA, cudaGetErrorString(e));
     return AFFT_GB300_ECUDA;
@@ -135,7 +310,12 @@ int afft_gb300_queue_run(afft_gb300_queue* q, void* stream) {
   return 0;
 }
 
-int afft_gb300_queue_launches(const afft_gb300_queue* q) { return q ? q->impl.launches : -1; }
+int afft_gb300_queue_launches(const afft_gb300_queue* q) {
+  if (!q) return -1;
+  int n = 0;
+  for (const auto& g : q->impl.groups) n += g.total > 0;
+  return n;
+}
 
 void afft_gb300_queue_destroy(afft_gb300_queue* q) { delete q; }
 

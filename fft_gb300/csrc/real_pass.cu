@@ -26,9 +26,8 @@ __device__ __forceinline__ float2 pre_one(float2 s0, float2 s1, float2 w) {
   return cadd(a, cmul_negi(b));
 }
 
-__global__ void real_pass_kernel(const RealPassParams p) {
+__device__ __forceinline__ void real_pass_body(const RealPassParams& p, long long idx) {
   const long long half = p.L / 2 + 1;
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   long long q, k;
   if (p.lines_fastest) {
     q = idx % p.nlines;
@@ -77,8 +76,7 @@ __global__ void real_pass_kernel(const RealPassParams p) {
   }
 }
 
-__global__ void copy_lines_kernel(const CopyParams p) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void copy_body(const CopyParams& p, long long idx) {
   if (idx >= p.nlines * p.len) return;
   const long long q = idx / p.len, i = idx - q * p.len;
   const long long a = line_off(p.in, q) + i * p.in.es;
@@ -87,8 +85,7 @@ __global__ void copy_lines_kernel(const CopyParams p) {
   p.out.im[b] = p.in.im[a];
 }
 
-__global__ void real1_kernel(const RealPassParams p) {
-  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void real1_body(const RealPassParams& p, long long q) {
   if (q >= p.nlines) return;
   const long long i = line_off(p.in, q), o = line_off(p.out, q);
   if (!p.inverse) {
@@ -96,6 +93,34 @@ __global__ void real1_kernel(const RealPassParams p) {
     p.out.im[o] = 0.f;
   } else {
     p.out.re[o] = p.in.re[i];
+  }
+}
+
+__global__ void real_pass_kernel(const RealPassParams p) {
+  real_pass_body(p, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+__global__ void copy_lines_kernel(const CopyParams p) {
+  copy_body(p, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+__global__ void real1_kernel(const RealPassParams p) {
+  real1_body(p, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+__global__ void elementwise_grouped(const EwSegment* __restrict__ segs, int nseg, long long total) {
+  for (long long v = blockIdx.x; v < total; v += gridDim.x) {
+    int lo = 0, hi = nseg - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (segs[mid].blk0 <= v) lo = mid;
+      else hi = mid - 1;
+    }
+    const EwSegment& s = segs[lo];
+    const long long idx = (v - s.blk0) * blockDim.x + threadIdx.x;
+    if (s.type == EW_REAL) real_pass_body(s.rp, idx);
+    else if (s.type == EW_COPY) copy_body(s.cp, idx);
+    else real1_body(s.rp, idx);
   }
 }
 
