@@ -291,8 +291,8 @@ class Queue:
         for i, (kind, dims, sr, si, dr, di) in enumerate(items):
             d = arr[i]
             d.kind = KINDS[kind] if isinstance(kind, str) else kind
-            d.ndim = len(dims)
-            for j, x in enumerate(dims):
+            d.ndim = len(dims)   # the library rejects ndim outside 1..3
+            for j, x in enumerate(dims[:3]):
                 d.dim[j] = int(x)
             d.src_re, d.src_im, d.dst_re, d.dst_im = ptr(sr), ptr(si), ptr(dr), ptr(di)
         self._q = lib().afft_gb300_queue_create(arr, len(items))
