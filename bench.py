@@ -139,6 +139,11 @@ def dist_env():
     return world, rank, local
 
 
+def rank_seed(rank):
+    """Each rank transforms its own batch: a distinct input seed per rank."""
+    return 1234 + rank
+
+
 def make_inputs(kind, dims, batch, seed, dev):
     import torch
     n = int(np.prod(dims))
@@ -284,7 +289,7 @@ def run_ours(args, cfg):
         desc = desc + " (batch overridden to %d)" % batch
     fwd = G.BatchPlan(kind, dims, batch)
     inv = G.BatchPlan("ci" if kind == "c" else "ri", dims, batch) if with_inv else None
-    src, mid, back = make_inputs(kind, dims, batch, 1234 + rank, dev)
+    src, mid, back = make_inputs(kind, dims, batch, rank_seed(rank), dev)
     stream = torch.cuda.Stream(device=dev)   # our kernels and the events share it
     torch.cuda.synchronize()
 
