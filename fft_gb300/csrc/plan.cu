@@ -121,6 +121,21 @@ static std::vector<float2> stage_table_dispatch(int logl, std::integer_sequence<
   return out;
 }
 
+std::vector<float2> stage_table_host(int logl) {
+  return stage_table_dispatch(logl, std::make_integer_sequence<int, 15>{});
+}
+
+void fourstep_table_host(long long N, std::vector<float2>* hi, std::vector<float2>* lo, int* lo_bits) {
+  int lb = 0;
+  while ((1LL << (2 * lb)) < N) lb++;
+  long long nlo = 1LL << lb, nhi = (N + nlo - 1) / nlo;
+  hi->resize(nhi);
+  lo->resize(nlo);
+  for (long long j = 0; j < nhi; j++) (*hi)[j] = root_f(j * nlo, N);
+  for (long long j = 0; j < nlo; j++) (*lo)[j] = root_f(j, N);
+  *lo_bits = lb;
+}
+
 const float2* stage_twiddles(int logl) {
   return upload(0, logl, stage_table_dispatch(logl, std::make_integer_sequence<int, 15>{}));
 }

@@ -98,5 +98,8 @@ int validate_shape(int ndim, const size_t* dim, int* ndim_out, long long* dims_o
 const float2* stage_twiddles(int logl);
 const float2* real_twiddles(long long L);         // W_{2L}^k, k < L
 void fourstep_tables(long long N, const float2** hi, const float2** lo, int* lo_bits);
+// The same tables on the host, without touching the device.
+std::vector<float2> stage_table_host(int logl);
+void fourstep_table_host(long long N, std::vector<float2>* hi, std::vector<float2>* lo, int* lo_bits);
 
 }  // namespace agb

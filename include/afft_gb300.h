@@ -201,6 +201,22 @@ AFFT_GB300_API size_t afft_gb300_plan_describe(int kind, size_t ndim,
 /* Number of this library's kernel launches one transform of `plan` issues. */
 AFFT_GB300_API int afft_gb300_plan_launches(const void* plan);
 
+/* Batched 1D complex transform that allocates nothing -- no counterpart in
+ * the reference.  For callers that cannot allocate device memory at call
+ * time (a device memory budget fixed at start-up, a custom allocator that
+ * owns the free memory, or loops that cannot take cudaMalloc's implicit
+ * synchronisation).  Runs the two-pass transform of `batch` dense lengths
+ * `n` (forward, or unnormalised inverse when `inverse` is nonzero) from
+ * src to dst (device pointers) on `stream` without waiting, with its scratch
+ * in a fixed 16 MiB device array inside the library.  Limits: n a power of
+ * two in [2^15, 2^21] and n * batch <= 2^21, else AFFT_GB300_EINVAL.  The
+ * first call on each device sets up the library's device arrays (make it
+ * before any stream capture); calls share the scratch array, so calls whose
+ * kernels overlap on the GPU race.  Returns 0 or an AFFT_GB300_* code. */
+AFFT_GB300_API int afft_gb300_c2c_noalloc(const float* src_re,
+  const float* src_im, float* dst_re, float* dst_im, size_t n, size_t batch,
+  int inverse, void* stream);
+
 /* Descriptor of one transform in a multi-transform queue.  dims beyond ndim
  * are ignored.  Pointers are device pointers.  For 'ci' and 'ri' the output
  * is unnormalised as above. */
