@@ -23,6 +23,7 @@ LIB_PATH = os.path.join(_HERE, "libafft_gb300.so")
 afft_auto, afft_scalar, afft_sse2, afft_avx2, afft_avx512f, afft_neon, afft_gb300 = range(7)
 afft_split, afft_interleaved = 0, 1
 KIND_C, KIND_CI, KIND_R, KIND_RI = 0, 1, 2, 3
+FORM_TC = 0x100   # AFFT_GB300_FORM_TC: split-precision tensor-core butterflies
 KINDS = {"c": KIND_C, "ci": KIND_CI, "r": KIND_R, "ri": KIND_RI}
 ERRORS = {0: "OK", 1: "EINVAL", 2: "ENODEV", 3: "ENOMEM", 4: "ECUDA", 5: "ESTATE", 6: "ETIMEOUT"}
 
@@ -79,6 +80,12 @@ def lib():
         L.afft_gb300_plan_launches.argtypes = [P]
         L.afft_gb300_queue_create.restype = P
         L.afft_gb300_queue_create.argtypes = [P, S]
+        L.afft_gb300_queue_create_ex.restype = P
+        L.afft_gb300_queue_create_ex.argtypes = [P, S, I]
+        L.afft_gb300_plan_describe.restype = S
+        L.afft_gb300_plan_describe.argtypes = [I, S, P, S, I, ctypes.c_char_p, S]
+        L.afft_gb300_c2c_noalloc.restype = I
+        L.afft_gb300_c2c_noalloc.argtypes = [P, P, P, P, S, S, I, P]
         L.afft_gb300_queue_run.restype = I
         L.afft_gb300_queue_run.argtypes = [P, P]
         L.afft_gb300_queue_launches.restype = I
@@ -227,12 +234,17 @@ class BatchPlan:
     stream (device pointers only) and returns immediately.
     """
 
-    def __init__(self, kind, dims, batch, fmt=afft_split):
+    def __init__(self, kind, dims, batch, fmt=afft_split, form=None):
         L = lib()
         self.kind = KINDS[kind] if isinstance(kind, str) else kind
         self.dims = [int(d) for d in dims]
         self.batch = int(batch)
         self.format = fmt
+        self.form = form
+        if form == "tc":
+            fmt = fmt | FORM_TC
+        elif form not in (None, "plain"):
+            raise ValueError("form must be None, 'plain' or 'tc'")
         arr, n = _dims(self.dims)
         size = L.afft_gb300_batch_memsize(self.kind, n, arr, self.batch, fmt)
         self.state = None
@@ -285,7 +297,7 @@ class Queue:
     device arrays.
     """
 
-    def __init__(self, descs):
+    def __init__(self, descs, form=None):
         items = list(descs)
         arr = (Desc * max(1, len(items)))()
         for i, (kind, dims, sr, si, dr, di) in enumerate(items):
@@ -295,7 +307,7 @@ class Queue:
             for j, x in enumerate(dims[:3]):
                 d.dim[j] = int(x)
             d.src_re, d.src_im, d.dst_re, d.dst_im = ptr(sr), ptr(si), ptr(dr), ptr(di)
-        self._q = lib().afft_gb300_queue_create(arr, len(items))
+        self._q = lib().afft_gb300_queue_create_ex(arr, len(items), FORM_TC if form == "tc" else 0)
         if not self._q:
             _check("queue_create")
             raise AfftError("queue_create failed")

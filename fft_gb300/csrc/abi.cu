@@ -112,7 +112,8 @@ static size_t check_args(size_t ndim, const size_t* dim, int format, int impl, i
   return 1;
 }
 
-static size_t memsize_impl(int kind, size_t ndim, const size_t* dim, size_t batch, int format, int impl) {
+static size_t memsize_impl(int kind, size_t ndim, const size_t* dim, size_t batch, int format, int impl,
+                           int form = 0) {
   int nd;
   long long dims[64];
   size_t r = check_args(ndim, dim, format, impl, &nd, dims);
@@ -123,13 +124,13 @@ static size_t memsize_impl(int kind, size_t ndim, const size_t* dim, size_t batc
   }
   // build a throwaway plan so unsupported shapes fail here, as afft's
   // memsize is the call that reports them
-  auto P = build_plan(kind, nd, dims, (long long)batch, format);
+  auto P = build_plan(kind, nd, dims, (long long)batch, format, false, form);
   if (!P) return 0;
   return kPlanMem;
 }
 
 static void* create_impl(int kind, size_t ndim, const size_t* dim, size_t batch, int format, void* mem,
-                         int impl) {
+                         int impl, int form = 0) {
   int nd;
   long long dims[64];
   size_t r = check_args(ndim, dim, format, impl, &nd, dims);
@@ -138,7 +139,7 @@ static void* create_impl(int kind, size_t ndim, const size_t* dim, size_t batch,
     set_error(AFFT_GB300_EINVAL, "null mem or zero batch");
     return nullptr;
   }
-  auto P = build_plan(kind, nd, dims, (long long)batch, format);
+  auto P = build_plan(kind, nd, dims, (long long)batch, format, false, form);
   if (!P) return nullptr;
   if (cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking) != cudaSuccess) {
     cudaGetLastError();
@@ -172,6 +173,20 @@ static void io_elems(const Plan& P, long long* in_n, long long* out_n) {
   *out_n = P.out_elems * P.batch;
 }
 
+// A TC-form kernel whose bounded wait for its tensor-core results gave up
+// sets the device error word instead of hanging; report and clear it.
+static int check_tc_error(const Plan& P) {
+  if (P.form != FORM_TC) return 0;
+  int* w = tc_error_word();
+  int v = 0;
+  if (w && cudaMemcpy(&v, w, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess && v) {
+    cudaMemset(w, 0, sizeof(int));
+    set_error(AFFT_GB300_ETIMEOUT, "tensor-core stage wait timed out");
+    return AFFT_GB300_ETIMEOUT;
+  }
+  return 0;
+}
+
 static int transform_sync(void* plan, const float* sr, const float* si, float* dr, float* di) {
   clear_error();
   auto P = lookup(plan);
@@ -192,7 +207,7 @@ static int transform_sync(void* plan, const float* sr, const float* si, float* d
       set_error(AFFT_GB300_ECUDA, cudaGetErrorString(e));
       return AFFT_GB300_ECUDA;
     }
-    return 0;
+    return check_tc_error(*P);
   }
   // host data: stage through plan-owned device buffers.  A batch is cut
   // into chunks so the copy of chunk i+1 in, the transform of chunk i and the
@@ -262,7 +277,7 @@ static int transform_sync(void* plan, const float* sr, const float* si, float* d
     set_error(AFFT_GB300_ECUDA, cudaGetErrorString(e));
     return AFFT_GB300_ECUDA;
   }
-  return 0;
+  return check_tc_error(*P);
 }
 
 }  // namespace agb
@@ -362,7 +377,7 @@ size_t afft_gb300_batch_memsize(int kind, size_t ndim, const size_t* dim, size_t
     set_error(AFFT_GB300_EINVAL, "bad kind");
     return 0;
   }
-  return memsize_impl(kind, ndim, dim, batch, format, afft_auto);
+  return memsize_impl(kind, ndim, dim, batch, format & ~FORM_TC, afft_auto, format & FORM_TC);
 }
 
 void* afft_gb300_batch_create(int kind, size_t ndim, const size_t* dim, size_t batch, int format, void* mem) {
@@ -370,7 +385,7 @@ void* afft_gb300_batch_create(int kind, size_t ndim, const size_t* dim, size_t b
     set_error(AFFT_GB300_EINVAL, "bad kind");
     return nullptr;
   }
-  return create_impl(kind, ndim, dim, batch, format, mem, afft_auto);
+  return create_impl(kind, ndim, dim, batch, format & ~FORM_TC, mem, afft_auto, format & FORM_TC);
 }
 
 int afft_gb300_transform_async(void* plan, const float* sr, const float* si, float* dr, float* di,
@@ -407,12 +422,14 @@ size_t afft_gb300_plan_describe(int kind, size_t ndim, const size_t* dim, size_t
   clear_error();
   int nd;
   long long dims[64];
+  const int form = format & FORM_TC;
+  format &= ~FORM_TC;
   if (kind < 0 || kind > 3 || ndim > 64 || (ndim && !dim) || batch == 0 ||
       (format != afft_split && format != afft_interleaved) || validate_shape((int)ndim, dim, &nd, dims)) {
     set_error(AFFT_GB300_EINVAL, "bad arguments");
     return 0;
   }
-  auto P = build_plan(kind, nd, dims, (long long)batch, format, true);
+  auto P = build_plan(kind, nd, dims, (long long)batch, format, true, form);
   if (!P) return 0;
   std::string s = describe_plan(*P);
   if (buf && buflen) {

@@ -33,6 +33,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "tc_dft.cuh"
+
 namespace agb {
 
 enum LineKind { LK_C2C = 0, LK_R2C = 1, LK_C2R = 2 };
@@ -61,6 +63,8 @@ struct LineParams {
   int tw_lo_bits;
   const float2* rtw;        // real pass twiddles W_{2L}^k, k < L
   int inverse;              // swap re/im on load and store
+  const __half* tc_b;       // TC form: Mh then Ml, 32x32 FP16 each, [n][k]
+  int* err;                 // TC form: error word set when a bounded wait gives up
 };
 
 // ---------------------------------------------------------------------------
@@ -212,9 +216,9 @@ __device__ __forceinline__ float2 ldg2(const float2* p) { return __ldg(p); }
 // One Stockham stage: B = E/R butterflies per thread, butterfly b = t + T*u
 // reads slots u + B*r, applies W_{NS*R}^{r*(b mod NS)}, DFT-R, and either
 // scatters to shared memory (non-last) or keeps the canonical layout (last).
-template <int R, int NS, int E, int T, bool LAST, class SM>
+template <int R, int NS, int E, int T, bool LAST, bool TC, int NT, class SM>
 __device__ __forceinline__ void stage(float2 (&v)[E], int t, int c, const float2* tw, const SM& sm,
-                                      bool do_write) {
+                                      bool do_write, TcState* ts) {
   constexpr int B = E / R;
 #pragma unroll
   for (int u = 0; u < B; u++) {
@@ -227,7 +231,12 @@ __device__ __forceinline__ void stage(float2 (&v)[E], int t, int c, const float2
 #pragma unroll
       for (int r = 1; r < R; r++) x[r] = cmul(x[r], ldg2(tw + (r - 1) * NS + k));
     }
-    dft<R>(x);
+    if constexpr (TC && R == 16) {
+      static_assert(E == 16, "TC form: one butterfly per thread");
+      tc_dft16<NT>(x, threadIdx.x, *ts);
+    } else {
+      dft<R>(x);
+    }
     if constexpr (LAST) {
 #pragma unroll
       for (int r = 0; r < R; r++) v[u + B * r] = x[r];
@@ -243,11 +252,12 @@ __device__ __forceinline__ void stage(float2 (&v)[E], int t, int c, const float2
 
 // All stages; v holds the input in canonical layout on entry and the output
 // in canonical layout on exit.
-template <int LOGL, int C, bool COLS, bool WARP_ONLY, int S>
+template <int LOGL, int C, bool COLS, bool WARP_ONLY, int S, bool TC = false>
 __device__ __forceinline__ void run_stages(float2 (&v)[Sched<LOGL>::E], int t, int c, const float2* tw,
-                                           const Smem<Sched<LOGL>::L, C, COLS>& sm) {
+                                           const Smem<Sched<LOGL>::L, C, COLS>& sm, TcState* ts = nullptr) {
   using Sc = Sched<LOGL>;
   constexpr int E = Sc::E, T = Sc::T;
+  constexpr int NT = (Sc::T * C) / 128;
   if constexpr (S < Sc::NSTAGES) {
     constexpr int R = Sc::radix(S);
     constexpr int NS = Sc::ns(S);
@@ -257,13 +267,15 @@ __device__ __forceinline__ void run_stages(float2 (&v)[Sched<LOGL>::E], int t, i
 #pragma unroll
       for (int e = 0; e < E; e++) v[e] = sm.get(c, t + T * e);
     }
+    // everyone finished reading before the buffer is written again (the TC
+    // form writes its operand tiles there even in the last stage)
+    if constexpr (S > 0 && (!LAST || TC)) line_sync<WARP_ONLY && !TC>();
     if constexpr (!LAST) {
-      if constexpr (S > 0) line_sync<WARP_ONLY>();   // everyone finished reading
-      stage<R, NS, E, T, false>(v, t, c, tw + Sc::twoff(S), sm, true);
-      line_sync<WARP_ONLY>();                          // writes visible
-      run_stages<LOGL, C, COLS, WARP_ONLY, S + 1>(v, t, c, tw, sm);
+      stage<R, NS, E, T, false, TC, NT>(v, t, c, tw + Sc::twoff(S), sm, true, ts);
+      line_sync<WARP_ONLY && !TC>();                   // writes visible
+      run_stages<LOGL, C, COLS, WARP_ONLY, S + 1, TC>(v, t, c, tw, sm, ts);
     } else {
-      stage<R, NS, E, T, true>(v, t, c, tw + Sc::twoff(S), sm, false);
+      stage<R, NS, E, T, true, TC, NT>(v, t, c, tw + Sc::twoff(S), sm, false, ts);
     }
   }
 }
@@ -290,13 +302,13 @@ constexpr int min_ctas() {
 }
 
 // The body of one CTA's work: lines [cta*C, cta*C + C) of the launch `p`.
-template <int LOGL, int C, bool COLS, int KIND, bool TSTORE>
-__device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta) {
+template <int LOGL, int C, bool COLS, int KIND, bool TSTORE, bool TC = false>
+__device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta, TcState* ts = nullptr) {
   using Sc = Sched<LOGL>;
   constexpr int L = Sc::L, E = Sc::E, T = Sc::T;
   // a line lives inside one warp: rows mode with T <= 32, or a single line
   constexpr bool WARP_ONLY = (!COLS && T <= 32) || (T * C <= 32);
-  extern __shared__ float2 smem_raw[];
+  extern __shared__ __align__(1024) float2 smem_raw[];
   Smem<L, C, COLS> sm{smem_raw};
 
   const int tid = threadIdx.x;
@@ -353,7 +365,7 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
     }
   }
 
-  run_stages<LOGL, C, COLS, WARP_ONLY, 0>(v, t, c, p.tw, sm);
+  run_stages<LOGL, C, COLS, WARP_ONLY, 0, TC>(v, t, c, p.tw, sm, ts);
 
   if constexpr (KIND == LK_C2C) {
     if (p.tw_n) {
@@ -438,10 +450,61 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
   }
 }
 
-template <int LOGL, int C, bool COLS, int KIND, bool TSTORE>
+// Per-CTA set-up of the TC form: TMEM columns (64 per 128-row tile), the
+// mbarrier and the DFT matrix tiles Mh, Ml in the K-major core layout.
+template <int NTHREADS>
+__device__ __forceinline__ void tc_setup(TcState& S, const LineParams& p, unsigned char* bt,
+                                         uint64_t* mbar, uint32_t* tmem_slot, float2* exch) {
+  constexpr int NT = NTHREADS / 128;
+  constexpr int COLS = NT * 64;   // 128 or 256: a power of two as tcgen05.alloc needs
+  static_assert(NT == 2 || NT == 4, "TC form: 256 or 512 threads");
+  const int tid = threadIdx.x;
+  if (tid < 256) {
+    const int mat = tid >> 7, n = (tid & 127) >> 2, g = tid & 3;
+    *(uint4*)(bt + mat * 2048 + tc_core_off(n, 8 * g)) = *(const uint4*)(p.tc_b + mat * 1024 + n * 32 + 8 * g);
+  }
+  if (tid < 32) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "n"(COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)));
+  asm volatile("fence.proxy.async.shared::cta;");
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  S.a = (unsigned char*)exch;
+  S.b = bt;
+  S.mbar = smem_u32(mbar);
+  S.tmem = *tmem_slot;
+  S.phase = 0;
+  S.err = p.err;
+}
+
+template <int NTHREADS>
+__device__ __forceinline__ void tc_teardown(const TcState& S) {
+  constexpr int COLS = (NTHREADS / 128) * 64;
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  if (threadIdx.x < 32) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(S.tmem), "n"(COLS));
+}
+
+template <int LOGL, int C, bool COLS, int KIND, bool TSTORE, bool TC = false>
 __global__ void __launch_bounds__(Sched<LOGL>::T * C, min_ctas<Sched<LOGL>::T * C>())
 line_fft(const LineParams p) {
-  line_fft_body<LOGL, C, COLS, KIND, TSTORE>(p, blockIdx.x);
+  if constexpr (TC) {
+    __shared__ __align__(1024) unsigned char bt[4096];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_slot;
+    extern __shared__ __align__(1024) float2 smem_raw[];
+    TcState S;
+    tc_setup<Sched<LOGL>::T * C>(S, p, bt, &mbar, &tmem_slot, smem_raw);
+    line_fft_body<LOGL, C, COLS, KIND, TSTORE, true>(p, blockIdx.x, &S);
+    tc_teardown<Sched<LOGL>::T * C>(S);
+  } else {
+    line_fft_body<LOGL, C, COLS, KIND, TSTORE>(p, blockIdx.x);
+  }
 }
 
 // One launch of a multi-transform queue: a device-side table of segments
@@ -454,10 +517,32 @@ struct Segment {
   long long cta0;
 };
 
-template <int LOGL, int C, bool COLS, int KIND, bool TSTORE>
+template <int LOGL, int C, bool COLS, int KIND, bool TSTORE, bool TC = false>
 __global__ void __launch_bounds__(Sched<LOGL>::T * C, min_ctas<Sched<LOGL>::T * C>())
 line_fft_grouped(const Segment* __restrict__ segs, int nseg, long long total) {
   __shared__ LineParams sp;
+  if constexpr (TC) {
+    __shared__ __align__(1024) unsigned char bt[4096];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_slot;
+    extern __shared__ __align__(1024) float2 smem_raw[];
+    TcState S;
+    tc_setup<Sched<LOGL>::T * C>(S, segs[0].p, bt, &mbar, &tmem_slot, smem_raw);
+    for (long long v = blockIdx.x; v < total; v += gridDim.x) {
+      int lo = 0, hi = nseg - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (segs[mid].cta0 <= v) lo = mid;
+        else hi = mid - 1;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) sp = segs[lo].p;
+      __syncthreads();
+      line_fft_body<LOGL, C, COLS, KIND, TSTORE, true>(sp, v - segs[lo].cta0, &S);
+    }
+    tc_teardown<Sched<LOGL>::T * C>(S);
+    return;
+  }
   for (long long v = blockIdx.x; v < total; v += gridDim.x) {
     int lo = 0, hi = nseg - 1;
     while (lo < hi) {

@@ -16,6 +16,8 @@
 //    pass with the fused real pass, and the complex (N-1)-D transform of each
 //    of the d0/2+1 planes in place on dst (reverse order for the inverse,
 //    through scratch).
+#include <cuda_fp16.h>
+
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -146,6 +148,54 @@ const float2* real_twiddles(long long L) {
   return upload(1, L, t);
 }
 
+// The real 32x32 DFT-16 matrix M = [[Wr, Wi], [-Wi, Wr]] of the TC form,
+// stored [n][k] (K-major B operand), as Mh = fp16(M) then
+// Ml = fp16((M - Mh) * 2048); entries computed in FP64.
+const __half* tc_matrix_table() {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  static std::mutex mu;
+  static std::map<int, __half*> tabs;
+  std::lock_guard<std::mutex> g(mu);
+  auto it = tabs.find(dev);
+  if (it != tabs.end()) return it->second;
+  std::vector<__half> h(2048);
+  for (int kk = 0; kk < 32; kk++)      // K index: input row (re 0..15, im 16..31)
+    for (int nn = 0; nn < 32; nn++) {  // N index: output (re 0..15, im 16..31)
+      int n = kk & 15, k = nn & 15;
+      double c, sn;
+      unit_root((long long)n * k, 16, &c, &sn);  // exp(-2 pi i nk/16) = c + i sn
+      double m;
+      if (kk < 16 && nn < 16) m = c;            // Xr -> Yr
+      else if (kk >= 16 && nn < 16) m = -sn;    // Xi -> Yr
+      else if (kk < 16) m = sn;                 // Xr -> Yi
+      else m = c;                               // Xi -> Yi
+      __half mh = __double2half(m);
+      h[nn * 32 + kk] = mh;
+      h[1024 + nn * 32 + kk] = __double2half((m - (double)__half2float(mh)) * 2048.0);
+    }
+  __half* d = nullptr;
+  if (cudaMalloc(&d, 2048 * sizeof(__half)) != cudaSuccess) return nullptr;
+  cudaMemcpy(d, h.data(), 2048 * sizeof(__half), cudaMemcpyHostToDevice);
+  tabs[dev] = d;
+  return d;
+}
+
+int* tc_error_word() {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  static std::mutex mu;
+  static std::map<int, int*> words;
+  std::lock_guard<std::mutex> g(mu);
+  auto it = words.find(dev);
+  if (it != words.end()) return it->second;
+  int* d = nullptr;
+  if (cudaMalloc(&d, sizeof(int)) != cudaSuccess) return nullptr;
+  cudaMemset(d, 0, sizeof(int));
+  words[dev] = d;
+  return d;
+}
+
 void fourstep_tables(long long N, const float2** hi, const float2** lo, int* lo_bits) {
   int lb = 0;
   while ((1LL << (2 * lb)) < N) lb++;  // lo covers about sqrt(N) entries
@@ -222,7 +272,8 @@ struct Builder {
     if (!ok) return;
     Op op;
     op.type = OP_LINE;
-    if (!get_line_kernel(logl, cols, kind, tstore, &op.k)) {
+    bool tc = P.form == FORM_TC && kind == LK_C2C && get_tc_kernel(logl, cols, tstore, &op.k);
+    if (!tc && !get_line_kernel(logl, cols, kind, tstore, &op.k)) {
       fail("no kernel for this line length");
       return;
     }
@@ -245,6 +296,14 @@ struct Builder {
       op.p.tw = stage_twiddles(logl);
       if (tw_n) fourstep_tables(tw_n, &op.p.tw_hi, &op.p.tw_lo, &op.p.tw_lo_bits);
       if (real_L) op.p.rtw = real_twiddles(real_L);
+      if (tc) {
+        op.p.tc_b = tc_matrix_table();
+        op.p.err = tc_error_word();
+        if (!op.p.tc_b || !op.p.err) {
+          fail("tensor-core table allocation failed");
+          return;
+        }
+      }
     }
     op.grid = (nlines + op.k.lines_per_cta - 1) / op.k.lines_per_cta;
     op.threads = op.k.threads;
@@ -388,10 +447,11 @@ struct Builder {
 };
 
 std::unique_ptr<Plan> build_plan(int kind, int ndim, const long long* dims, long long batch, int format,
-                                 bool dry) {
+                                 bool dry, int form) {
   std::unique_ptr<Plan> P(new Plan());
   P->kind = kind;
   P->format = format;
+  P->form = form;
   P->ndim = ndim;
   for (int i = 0; i < ndim; i++) P->dims[i] = dims[i];
   P->batch = batch;
@@ -535,11 +595,11 @@ std::string describe_plan(const Plan& P) {
     if (i) o += ",";
     if (op.type == OP_LINE) {
       snprintf(buf, sizeof buf,
-               "{\"type\":\"line\",\"logl\":%d,\"cols\":%d,\"lk\":%d,\"tstore\":%d,\"C\":%d,"
+               "{\"type\":\"line\",\"logl\":%d,\"cols\":%d,\"lk\":%d,\"tstore\":%d,\"tc\":%d,\"C\":%d,"
                "\"threads\":%d,\"smem\":%zu,\"grid\":%lld,\"nlines\":%lld,\"inverse\":%d,"
                "\"tw_n\":%lld,\"tw_qmask\":%lld,\"tw_qshift\":%d,\"real_L\":%lld,",
-               op.k.logl, op.k.cols, op.k.kind, op.k.tstore, op.k.lines_per_cta, op.threads, op.smem, op.grid,
-               op.p.nlines, op.p.inverse, op.p.tw_n, op.p.tw_qmask, op.p.tw_qshift, op.real_L);
+               op.k.logl, op.k.cols, op.k.kind, op.k.tstore, op.k.tc, op.k.lines_per_cta, op.threads, op.smem,
+               op.grid, op.p.nlines, op.p.inverse, op.p.tw_n, op.p.tw_qmask, op.p.tw_qshift, op.real_L);
     } else if (op.type == OP_REAL) {
       snprintf(buf, sizeof buf,
                "{\"type\":\"real\",\"threads\":%d,\"grid\":%lld,\"nlines\":%lld,\"L\":%lld,"

@@ -51,9 +51,14 @@ struct Op {
 void set_error(int code, const std::string& msg);
 void clear_error();
 
+// Form flag, OR-ed into the format argument of the batched and describe
+// entry points: split-precision tensor-core butterflies where eligible.
+constexpr int FORM_TC = 0x100;
+
 struct Plan {
   int kind = K_C;
   int format = 0;              // afft_split / afft_interleaved
+  int form = 0;                // 0 plain FP32, FORM_TC split-precision tensor cores
   int ndim = 1;
   long long dims[64] = {0};
   long long batch = 1;
@@ -86,7 +91,10 @@ struct Plan {
 // dry: build the op list only (no device calls, twiddle pointers null), for
 // describing a plan without a GPU.
 std::unique_ptr<Plan> build_plan(int kind, int ndim, const long long* dims, long long batch,
-                                 int format, bool dry = false);
+                                 int format, bool dry = false, int form = 0);
+// TC form: the DFT-16 matrix tiles (Mh, Ml) and the per-device error word
+const __half* tc_matrix_table();
+int* tc_error_word();
 
 // JSON description of a plan's ops (kernel shapes, grids, address specs).
 std::string describe_plan(const Plan& P);

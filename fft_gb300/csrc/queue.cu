@@ -38,6 +38,7 @@ struct Group {
 };
 
 struct QueueImpl {
+  int form = 0;
   std::vector<afft_gb300_desc> descs;
   std::map<std::vector<long long>, std::shared_ptr<Plan>> plans;
   std::vector<Group> groups;
@@ -88,7 +89,7 @@ static int build_queue(QueueImpl& Q) {
     key.insert(key.end(), dims, dims + nd);
     auto it = Q.plans.find(key);
     if (it == Q.plans.end()) {
-      auto P = build_plan(d.kind, nd, dims, 1, 0);
+      auto P = build_plan(d.kind, nd, dims, 1, 0, false, Q.form);
       if (!P) return AFFT_GB300_EINVAL;
       it = Q.plans.emplace(key, std::shared_ptr<Plan>(P.release())).first;
     }
@@ -267,6 +268,10 @@ struct afft_gb300_queue {
 extern "C" {
 
 afft_gb300_queue* afft_gb300_queue_create(const afft_gb300_desc* descs, size_t count) {
+  return afft_gb300_queue_create_ex(descs, count, 0);
+}
+
+afft_gb300_queue* afft_gb300_queue_create_ex(const afft_gb300_desc* descs, size_t count, int flags) {
   clear_error();
   if (!descs && count) {
     set_error(AFFT_GB300_EINVAL, "null descriptor array");
@@ -274,6 +279,7 @@ afft_gb300_queue* afft_gb300_queue_create(const afft_gb300_desc* descs, size_t c
   }
   auto* q = new afft_gb300_queue();
   QueueImpl& Q = q->impl;
+  Q.form = flags & FORM_TC;
   cudaGetDevice(&Q.device);
   Q.descs.assign(descs, descs + count);
   if (cudaStreamCreateWithFlags(&Q.stream, cudaStreamNonBlocking) != cudaSuccess) {

@@ -167,6 +167,14 @@ AFFT_GB300_API const char* afft_gb300_last_error_string(void);
 /* Kinds for the batched and queue entry points. */
 enum { afft_gb300_c = 0, afft_gb300_ci = 1, afft_gb300_r = 2, afft_gb300_ri = 3 };
 
+/* Form flag, OR-ed into `format` of afft_gb300_batch_memsize/_create and
+ * afft_gb300_plan_describe, or passed to afft_gb300_queue_create_ex:
+ * radix-16 butterflies of complex passes of length 256 and 4096 run as
+ * split-precision tensor-core DFT-matrix products (FP16 hi + scaled lo
+ * operands, three products accumulated in FP32 in TMEM); other passes keep
+ * the FP32 butterflies.  Accuracy bound: rel-L2 <= 5e-6 vs FP64. */
+enum { AFFT_GB300_FORM_TC = 0x100 };
+
 /* Batched plans: `batch` transforms of the same shape, dense and back to
  * back (transform b at offset b*in_elems / b*out_elems of each array, where
  * in/out_elems are prod(dims) for complex and (d0/2+1)*prod(dims[1:]) for
@@ -238,6 +246,9 @@ typedef struct afft_gb300_desc
 typedef struct afft_gb300_queue afft_gb300_queue;
 AFFT_GB300_API afft_gb300_queue* afft_gb300_queue_create(const afft_gb300_desc* descs,
   size_t count);
+/* As afft_gb300_queue_create; flags: 0 or AFFT_GB300_FORM_TC. */
+AFFT_GB300_API afft_gb300_queue* afft_gb300_queue_create_ex(
+  const afft_gb300_desc* descs, size_t count, int flags);
 /* `stream` as for afft_gb300_transform_async (NULL = default stream). */
 AFFT_GB300_API int afft_gb300_queue_run(afft_gb300_queue* q, void* stream);
 /* Kernel launches one run issues (after grouping). */

@@ -29,6 +29,7 @@ SRC_RE, SRC_IM, DST_RE, DST_IM, SCR = range(5)
 
 
 def describe(kind, dims, batch=1, fmt=0):
+    """fmt may carry fft_gb300.FORM_TC."""
     L = G.lib()
     f = L.afft_gb300_plan_describe
     f.restype = ctypes.c_size_t
