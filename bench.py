@@ -50,6 +50,10 @@ CONFIGS = {
 }
 
 
+FORMS = {"plain": "plain FP32 Stockham",
+         "tc": "split-precision tensor cores (tcgen05 DFT-16, FP16 hi+lo, FP32 accumulate) where eligible"}
+
+
 def peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -232,7 +236,7 @@ def run_queue(args, desc):
     dev = torch.device("cuda", 0)
     items = U.uneven_batch(args.batch or 10000, seed=5)
     buf, offs = U.allocate(items, dev)
-    q = G.Queue(U.descs(items, buf, offs))
+    q = G.Queue(U.descs(items, buf, offs), form=None if args.form == "plain" else args.form)
     stream = torch.cuda.Stream(device=dev)
     for _ in range(max(args.warmup, 3)):
         q.run(stream)
@@ -259,7 +263,7 @@ def run_queue(args, desc):
         "warmup": max(args.warmup, 3), "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded standard normal)",
         "config": {"workload": desc, "transforms": len(items), "transforms_per_s": round(len(items) / (ms / 1e3), 1),
-                   "form": "plain FP32 Stockham", "algorithmic_bytes": by, "queue_launches": q.launches},
+                   "form": FORMS[args.form], "algorithmic_bytes": by, "queue_launches": q.launches},
         "roofline": {"bound": "hbm", "achieved": round(by / (ms / 1e3) / 1e9, 1), "peak": hbm, "unit": "GB/s",
                      "frac": round(by / (ms / 1e3) / 1e9 / hbm, 4), "traffic": args.traffic,
                      "peak_source": peak_src, "kernel": "whole queue (graph of %d launches)" % q.launches},
@@ -287,8 +291,9 @@ def run_ours(args, cfg):
     if args.batch:
         batch = args.batch
         desc = desc + " (batch overridden to %d)" % batch
-    fwd = G.BatchPlan(kind, dims, batch)
-    inv = G.BatchPlan("ci" if kind == "c" else "ri", dims, batch) if with_inv else None
+    form = None if args.form == "plain" else args.form
+    fwd = G.BatchPlan(kind, dims, batch, form=form)
+    inv = G.BatchPlan("ci" if kind == "c" else "ri", dims, batch, form=form) if with_inv else None
     src, mid, back = make_inputs(kind, dims, batch, rank_seed(rank), dev)
     stream = torch.cuda.Stream(device=dev)   # our kernels and the events share it
     torch.cuda.synchronize()
@@ -374,7 +379,7 @@ def run_ours(args, cfg):
         "warmup": max(args.warmup, 3), "ms_per_step": round(ms_step, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded standard normal)",
         "config": {"workload": desc, "kind": kind, "dims": dims, "batch_per_gpu": batch,
-                   "form": "plain FP32 Stockham", "l2": "inputs larger than L2 (512 MiB per array pair)"
+                   "form": FORMS[args.form], "l2": "inputs larger than L2 (512 MiB per array pair)"
                    if bytes_of(kind, dims, batch) > 2 * 129e6 else "working set may fit L2",
                    "parallelism": "dp%d (independent batches)" % world},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
@@ -448,6 +453,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
     ap.add_argument("--batch", type=int, default=0, help="override the batch (profiling a smaller case)")
+    ap.add_argument("--form", default="plain", choices=["plain", "tc"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=10.0)

@@ -16,6 +16,7 @@ struct LineKernel {
   int kind;            // LK_C2C / LK_R2C / LK_C2R
   int tstore;          // store with the along-line mapping (four-step pass A)
   int tc;              // split-precision tensor-core butterflies
+  int unit;            // unit element strides specialised (rows c2c)
   int lines_per_cta;   // C
   int threads;         // T * C
   size_t smem;         // bytes of dynamic shared memory
@@ -26,6 +27,8 @@ constexpr int COLS_MAX_LOG = 11;   // cols mode: one CTA up to 2048 points
 
 // rows: kind in {LK_C2C, LK_R2C, LK_C2R}; cols: tstore only with LK_C2C
 bool get_line_kernel(int logl, bool cols, int kind, bool tstore, LineKernel* out);
+// rows c2c with unit element strides (split data): compile-time offsets
+bool get_rows_c2c_unit(int logl, bool tc, LineKernel* out);
 
 // split-precision tensor-core form: rows c2c L = 256 or 4096, cols c2c L = 256
 bool get_tc_kernel(int logl, bool cols, bool tstore, LineKernel* out);
@@ -44,16 +47,17 @@ constexpr int lines_per_cta() {
   else return T >= 256 ? 1 : 256 / T;
 }
 
-template <int LOGL, bool COLS, int KIND, bool TSTORE, bool TC = false>
+template <int LOGL, bool COLS, int KIND, bool TSTORE, bool TC = false, bool UNIT = false>
 LineKernel make_line_kernel() {
   constexpr int C = lines_per_cta<LOGL, COLS>();
   constexpr int L = 1 << LOGL;
   static_assert(!TC || (size_t)Smem<L, C, COLS>::FLOAT2S * 8 >= (size_t)(Sched<LOGL>::T * C / 128) * 16384,
                 "TC operand tiles must fit in the exchange buffer");
   LineKernel k;
-  k.fn = &line_fft<LOGL, C, COLS, KIND, TSTORE, TC>;
-  k.grouped = &line_fft_grouped<LOGL, C, COLS, KIND, TSTORE, TC>;
+  k.fn = &line_fft<LOGL, C, COLS, KIND, TSTORE, TC, UNIT>;
+  k.grouped = &line_fft_grouped<LOGL, C, COLS, KIND, TSTORE, TC, UNIT>;
   k.tc = TC;
+  k.unit = UNIT;
   k.logl = LOGL;
   k.cols = COLS;
   k.kind = KIND;

@@ -302,7 +302,9 @@ constexpr int min_ctas() {
 }
 
 // The body of one CTA's work: lines [cta*C, cta*C + C) of the launch `p`.
-template <int LOGL, int C, bool COLS, int KIND, bool TSTORE, bool TC = false>
+// UNIT: both element strides are 1 (split complex rows), so element offsets
+// are compile-time constants instead of runtime 64-bit products.
+template <int LOGL, int C, bool COLS, int KIND, bool TSTORE, bool TC = false, bool UNIT = false>
 __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta, TcState* ts = nullptr) {
   using Sc = Sched<LOGL>;
   constexpr int L = Sc::L, E = Sc::E, T = Sc::T;
@@ -350,10 +352,17 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
   } else {
     if (active) {
       const long long base = line_off(p.in, q);
+      if constexpr (UNIT) {
+        const float* pr = p.in.re + base + t;
+        const float* pi = p.in.im + base + t;
 #pragma unroll
-      for (int e = 0; e < E; e++) {
-        const long long a = base + (long long)(t + T * e) * p.in.es;
-        v[e] = make_float2(__ldg(p.in.re + a), __ldg(p.in.im + a));
+        for (int e = 0; e < E; e++) v[e] = make_float2(__ldg(pr + T * e), __ldg(pi + T * e));
+      } else {
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+          const long long a = base + (long long)(t + T * e) * p.in.es;
+          v[e] = make_float2(__ldg(p.in.re + a), __ldg(p.in.im + a));
+        }
       }
       if (p.inverse) {
 #pragma unroll
@@ -396,11 +405,21 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
       }
     } else if (active) {
       const long long base = line_off(p.out, q);
+      if constexpr (UNIT) {
+        float* pr = p.out.re + base + t;
+        float* pi = p.out.im + base + t;
 #pragma unroll
-      for (int e = 0; e < E; e++) {
-        const long long a = base + (long long)(t + T * e) * p.out.es;
-        p.out.re[a] = v[e].x;
-        p.out.im[a] = v[e].y;
+        for (int e = 0; e < E; e++) {
+          pr[T * e] = v[e].x;
+          pi[T * e] = v[e].y;
+        }
+      } else {
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+          const long long a = base + (long long)(t + T * e) * p.out.es;
+          p.out.re[a] = v[e].x;
+          p.out.im[a] = v[e].y;
+        }
       }
     }
   } else if constexpr (KIND == LK_C2R) {
@@ -490,7 +509,7 @@ __device__ __forceinline__ void tc_teardown(const TcState& S) {
   if (threadIdx.x < 32) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(S.tmem), "n"(COLS));
 }
 
-template <int LOGL, int C, bool COLS, int KIND, bool TSTORE, bool TC = false>
+template <int LOGL, int C, bool COLS, int KIND, bool TSTORE, bool TC = false, bool UNIT = false>
 __global__ void __launch_bounds__(Sched<LOGL>::T * C, min_ctas<Sched<LOGL>::T * C>())
 line_fft(const LineParams p) {
   if constexpr (TC) {
@@ -500,10 +519,10 @@ line_fft(const LineParams p) {
     extern __shared__ __align__(1024) float2 smem_raw[];
     TcState S;
     tc_setup<Sched<LOGL>::T * C>(S, p, bt, &mbar, &tmem_slot, smem_raw);
-    line_fft_body<LOGL, C, COLS, KIND, TSTORE, true>(p, blockIdx.x, &S);
+    line_fft_body<LOGL, C, COLS, KIND, TSTORE, true, UNIT>(p, blockIdx.x, &S);
     tc_teardown<Sched<LOGL>::T * C>(S);
   } else {
-    line_fft_body<LOGL, C, COLS, KIND, TSTORE>(p, blockIdx.x);
+    line_fft_body<LOGL, C, COLS, KIND, TSTORE, false, UNIT>(p, blockIdx.x);
   }
 }
 
@@ -517,7 +536,7 @@ struct Segment {
   long long cta0;
 };
 
-template <int LOGL, int C, bool COLS, int KIND, bool TSTORE, bool TC = false>
+template <int LOGL, int C, bool COLS, int KIND, bool TSTORE, bool TC = false, bool UNIT = false>
 __global__ void __launch_bounds__(Sched<LOGL>::T * C, min_ctas<Sched<LOGL>::T * C>())
 line_fft_grouped(const Segment* __restrict__ segs, int nseg, long long total) {
   __shared__ LineParams sp;
@@ -538,7 +557,7 @@ line_fft_grouped(const Segment* __restrict__ segs, int nseg, long long total) {
       __syncthreads();
       if (threadIdx.x == 0) sp = segs[lo].p;
       __syncthreads();
-      line_fft_body<LOGL, C, COLS, KIND, TSTORE, true>(sp, v - segs[lo].cta0, &S);
+      line_fft_body<LOGL, C, COLS, KIND, TSTORE, true, UNIT>(sp, v - segs[lo].cta0, &S);
     }
     tc_teardown<Sched<LOGL>::T * C>(S);
     return;
@@ -553,7 +572,7 @@ line_fft_grouped(const Segment* __restrict__ segs, int nseg, long long total) {
     __syncthreads();   // previous iteration done with sp and the staging buffers
     if (threadIdx.x == 0) sp = segs[lo].p;
     __syncthreads();
-    line_fft_body<LOGL, C, COLS, KIND, TSTORE>(sp, v - segs[lo].cta0);
+    line_fft_body<LOGL, C, COLS, KIND, TSTORE, false, UNIT>(sp, v - segs[lo].cta0);
   }
 }
 

@@ -273,7 +273,10 @@ struct Builder {
     Op op;
     op.type = OP_LINE;
     bool tc = P.form == FORM_TC && kind == LK_C2C && get_tc_kernel(logl, cols, tstore, &op.k);
-    if (!tc && !get_line_kernel(logl, cols, kind, tstore, &op.k)) {
+    const bool unit = !cols && !tstore && kind == LK_C2C && in.es == 1 && out.es == 1;
+    if (unit && get_rows_c2c_unit(logl, tc, &op.k)) {
+      // same kernel with compile-time element offsets
+    } else if (!tc && !get_line_kernel(logl, cols, kind, tstore, &op.k)) {
       fail("no kernel for this line length");
       return;
     }
