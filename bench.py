@@ -64,6 +64,16 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def measured_traffic(cfg):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu
+    summary (profiles/traffic.json), or None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            return json.load(f)[cfg]["dram_bytes_per_launch"]
+    except Exception:
+        return None
+
+
 def flops_of(kind, dims, batch):
     n = int(np.prod(dims))
     c = 5.0 if kind in ("c", "ci") else 2.5
@@ -383,7 +393,9 @@ def run_ours(args, cfg):
                    if bytes_of(kind, dims, batch) > 2 * 129e6 else "working set may fit L2",
                    "parallelism": "dp%d (independent batches)" % world},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-                     "frac": round(achieved / hbm, 4), "traffic": args.traffic, "peak_source": peak_src,
+                     "frac": round(achieved / hbm, 4),
+                     "traffic": args.traffic if args.traffic else (measured_traffic(cfg) if not args.batch and args.form == "plain" else None),
+                     "peak_source": peak_src,
                      "kernel": "forward plan (%d launch%s), %.4f ms per launch" % (
                          fwd.launches, "es" if fwd.launches > 1 else "", fwd_ms / fwd.launches)},
         "cpu_baseline": cpu,
