@@ -239,21 +239,6 @@ static View inter_view(int b, long long off = 0) {  // re,im pairs in one array
   return v;
 }
 
-// A view moved by `elems` complex elements.
-static View shifted(const View& v, long long elems) {
-  View r = v;
-  r.re.off += elems * v.unit;
-  r.im.off += elems * v.unit;
-  return r;
-}
-
-// Working-set size below which consecutive passes over the same data are run
-// chunk by chunk so the intermediate stays in the (126 MB) L2 cache.
-#ifndef AFFT_CHUNK_MB
-#define AFFT_CHUNK_MB 32
-#endif
-constexpr long long kChunkBytes = (long long)AFFT_CHUNK_MB << 20;
-
 static IOSpec io(const View& v, long long es, long long lo, long long hi, int qshift, long long qmask) {
   IOSpec s;
   s.re = v.re;
@@ -405,21 +390,15 @@ struct Builder {
         return;
       }
       long long L1 = 1LL << l1, L2 = 1LL << l2;
-      // transforms per chunk: pass B reads pass A's output while it is in L2
-      long long chunk = std::max(1LL, std::min(outer, kChunkBytes / (8 * L)));
       View S = split_view(B_SCR, B_SCR, scr_base);
-      S.im.off = scr_base + chunk * L;  // scratch: re block then im block
-      need_scratch(scr_base + 2 * chunk * L);
-      for (long long o0 = 0; o0 < outer; o0 += chunk) {
-        long long oc = std::min(chunk, outer - o0);
-        View Ac = shifted(A, o0 * a_bs), Bc = shifted(B, o0 * b_bs);
-        // pass A: lines (o, t2), points t1 -> Y[o][t2][k1] (transposed store)
-        line(LK_C2C, true, true, l1, io(Ac, L2, 1, a_bs, l2, L2 - 1), io(S, 1, L1, L, l2, L2 - 1),
-             oc * L2, inverse, L, L2 - 1, 0);
-        // pass B: lines (o, k1), points t2 -> X[o][k1 + L1 k2]
-        line(LK_C2C, true, false, l2, io(S, L1, 1, L, l1, L1 - 1), io(Bc, L1, 1, b_bs, l1, L1 - 1),
-             oc * L1, inverse);
-      }
+      S.im.off = scr_base + outer * L;  // scratch: re block then im block
+      need_scratch(scr_base + 2 * outer * L);
+      // pass A: lines (o, t2), points t1 -> Y[o][t2][k1] (transposed store)
+      line(LK_C2C, true, true, l1, io(A, L2, 1, a_bs, l2, L2 - 1), io(S, 1, L1, L, l2, L2 - 1),
+           outer * L2, inverse, L, L2 - 1, 0);
+      // pass B: lines (o, k1), points t2 -> X[o][k1 + L1 k2]
+      line(LK_C2C, true, false, l2, io(S, L1, 1, L, l1, L1 - 1), io(B, L1, 1, b_bs, l1, L1 - 1),
+           outer * L1, inverse);
       return;
     }
     int lin = ilog2ll(inner);
@@ -454,47 +433,6 @@ struct Builder {
     long long total = count;
     for (int i = 0; i < nd; i++) total *= dims[i];
     bool first = true;
-    // Trailing axes whose sub-arrays are small: all their passes run chunk by
-    // chunk (a chunk of consecutive sub-arrays stays in L2 between passes),
-    // then the leading axes run over the whole array.
-    int split = nd;
-    for (int j = nd - 1; j >= 1; j--) {
-      long long sub = 1;
-      int live = 0;
-      for (int i = j; i < nd; i++) {
-        sub *= dims[i];
-        live += dims[i] > 1;
-      }
-      if (8 * sub * 2 <= kChunkBytes && live >= 2) split = j;
-    }
-    if (split < nd) {
-      long long sub = 1;
-      for (int i = split; i < nd; i++) sub *= dims[i];
-      long long nsub = total / sub;
-      long long chunk = std::max(1LL, std::min(nsub, kChunkBytes / (8 * sub)));
-      for (long long s0 = 0; s0 < nsub; s0 += chunk) {
-        long long sc = std::min(chunk, nsub - s0);
-        bool cfirst = true;
-        for (int ax = nd - 1; ax >= split; ax--) {
-          long long L = dims[ax];
-          if (L == 1) continue;
-          long long inner = 1;
-          for (int j = ax + 1; j < nd; j++) inner *= dims[j];
-          long long outer = sc * sub / (L * inner);
-          axis(outer, L, inner, shifted(cfirst ? A : B, s0 * sub), shifted(B, s0 * sub), inverse);
-          cfirst = false;
-        }
-      }
-      first = false;
-      for (int ax = split - 1; ax >= 0; ax--) {
-        long long L = dims[ax];
-        if (L == 1) continue;
-        long long inner = 1;
-        for (int j = ax + 1; j < nd; j++) inner *= dims[j];
-        axis(total / (L * inner), L, inner, B, B, inverse);
-      }
-      return;
-    }
     for (int ax = nd - 1; ax >= 0; ax--) {
       long long L = dims[ax];
       if (L == 1) continue;
