@@ -32,6 +32,23 @@ void clear_error() {
   g_msg.clear();
 }
 
+// Makes the plan's device current for the duration of a call and restores
+// the caller's device afterwards.
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) {
+      cudaGetLastError();
+      prev = -1;
+    }
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+  }
+};
+
 static const uint64_t kMagic = 0x3030334247544641ULL;  // "AFTGB300"
 
 struct Header {
@@ -141,6 +158,14 @@ static void* create_impl(int kind, size_t ndim, const size_t* dim, size_t batch,
   }
   auto P = build_plan(kind, nd, dims, (long long)batch, format, false, form);
   if (!P) return nullptr;
+  // device scratch now, so later launches allocate nothing (and can be
+  // captured into CUDA graphs)
+  if (P->scratch_floats > 0 &&
+      cudaMalloc(&P->scratch, (size_t)P->scratch_floats * sizeof(float)) != cudaSuccess) {
+    cudaGetLastError();
+    set_error(AFFT_GB300_ENOMEM, "scratch allocation failed");
+    return nullptr;
+  }
   if (cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking) != cudaSuccess) {
     cudaGetLastError();
     set_error(AFFT_GB300_ECUDA, "stream creation failed");
@@ -192,7 +217,7 @@ static int transform_sync(void* plan, const float* sr, const float* si, float* d
   auto P = lookup(plan);
   if (!P) return AFFT_GB300_ESTATE;
   std::lock_guard<std::mutex> g(P->mu);
-  cudaSetDevice(P->device);
+  DeviceGuard dg(P->device);
   const bool real_in = P->kind == K_R, real_out = P->kind == K_RI;
   const bool inter = P->format == afft_interleaved;
   // arguments that carry data for this kind/format
@@ -394,7 +419,7 @@ int afft_gb300_transform_async(void* plan, const float* sr, const float* si, flo
   auto P = lookup(plan);
   if (!P) return AFFT_GB300_ESTATE;
   std::lock_guard<std::mutex> g(P->mu);
-  cudaSetDevice(P->device);
+  DeviceGuard dg(P->device);
   // NULL is the CUDA default stream, as for a kernel launch
   return P->launch(sr, si, dr, di, (cudaStream_t)stream);
 }

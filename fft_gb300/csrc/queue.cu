@@ -302,7 +302,15 @@ int afft_gb300_queue_run(afft_gb300_queue* q, void* stream) {
     return AFFT_GB300_EINVAL;
   }
   QueueImpl& Q = q->impl;
-  cudaSetDevice(Q.device);
+  int prev = -1;
+  cudaGetDevice(&prev);
+  if (prev != Q.device) cudaSetDevice(Q.device);
+  struct Restore {
+    int d, p;
+    ~Restore() {
+      if (p >= 0 && p != d) cudaSetDevice(p);
+    }
+  } restore{Q.device, prev};
   if (!Q.exec && capture(Q)) {
     cudaGetLastError();
     set_error(AFFT_GB300_ECUDA, "graph capture failed");

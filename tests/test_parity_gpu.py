@@ -355,3 +355,37 @@ def test_batch_host_pointers_pipelined(kind, dev):
         si, so = slice(j * in_n, (j + 1) * in_n), slice(j * out_n, (j + 1) * out_n)
         got = oa_n[so] if kind == "ri" else (oa_n[so], ob_n[so])
         check(kind, dims, a[si], None if b is None else b[si], got)
+
+
+def test_async_launch_captured_in_cuda_graph(dev):
+    # plans allocate their scratch at creation, so their launches can be
+    # recorded into a CUDA graph and replayed
+    n, batch = 1 << 17, 4   # four-step: uses scratch
+    rng = np.random.default_rng(31)
+    xr = torch.from_numpy(rng.standard_normal(n * batch).astype(np.float32)).to(dev)
+    xi = torch.from_numpy(rng.standard_normal(n * batch).astype(np.float32)).to(dev)
+    yr, yi = torch.zeros_like(xr), torch.zeros_like(xi)
+    plan = G.BatchPlan("c", [n], batch)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        plan.launch(xr, xi, yr, yi, stream=s)   # warm-up outside capture
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        plan.launch(xr, xi, yr, yi, stream=s)
+    yr.zero_()
+    yi.zero_()
+    g.replay()
+    torch.cuda.synchronize()
+    a, b = xr.cpu().numpy(), xi.cpu().numpy()
+    for j in (0, batch - 1):
+        sl = slice(j * n, (j + 1) * n)
+        check("c", [n], a[sl], b[sl], (yr.cpu().numpy()[sl], yi.cpu().numpy()[sl]))
+
+
+def test_caller_device_unchanged(dev):
+    torch.cuda.set_device(0)
+    p = G.complex_transform([256])
+    x = np.ones(256, np.float32)
+    p(x, x, np.zeros(256, np.float32), np.zeros(256, np.float32))
+    assert torch.cuda.current_device() == 0
