@@ -40,10 +40,14 @@ bool get_rows_c2r(int logl, LineKernel* out);
 bool get_cols_c2c(int logl, bool tstore, LineKernel* out);
 bool get_cols_real(int logl, int kind, LineKernel* out);
 
+// Lines per cols-mode CTA, measured per length on GB300: 32 lines up to
+// 128 points, 16 for 256 and 512 (256/512 threads, several CTAs per SM),
+// 8 for 1024 and 2048 (narrower tiles lose DRAM locality: 32-byte row
+// segments are the floor).
 template <int LOGL, bool COLS>
 constexpr int lines_per_cta() {
   constexpr int T = Sched<LOGL>::T;
-  if constexpr (COLS) return T <= 32 ? 32 : (T <= 64 ? 16 : 8);
+  if constexpr (COLS) return LOGL <= 7 ? 32 : (LOGL <= 9 ? 16 : 8);
   else return T >= 256 ? 1 : 256 / T;
 }
 
