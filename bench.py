@@ -366,6 +366,12 @@ def run_ours(args, cfg):
     value = per_step_flops * world / (ms_step / 1e3) / 1e9
     launches_per_step = fwd.launches + (inv.launches if inv else 0)
 
+    # the split-precision tensor-core form on the same workload, same stream
+    tc_form = None
+    if args.form == "plain" and not args.no_tc and world == 1:
+        tc_form = tc_form_rate(kind, dims, batch, with_inv, src, mid, back, stream, G, torch,
+                               per_step_flops, ms_step)
+
     # end to end through the C ABI with pinned host buffers
     e2e = None
     if not args.no_e2e:
@@ -400,12 +406,50 @@ def run_ours(args, cfg):
                          fwd.launches, "es" if fwd.launches > 1 else "", fwd_ms / fwd.launches)},
         "cpu_baseline": cpu,
         "e2e": e2e,
+        "tc_split_form": tc_form,
         "gpu_launches": launches_per_step * args.steps,
         "clocks": dict(clk.summary(), window="soak %.1f s + timed region" % args.soak),
     }
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def tc_form_rate(kind, dims, batch, with_inv, src, mid, back, stream, G, torch, per_step_flops, plain_ms):
+    """Same steps with the split-precision tensor-core form (AFFT_GB300_FORM_TC):
+    its rate, its ratio to the plain form, and its worst rel-L2 against the
+    plain FP32 result on a sample of transforms (the FP64 check is in the
+    tests)."""
+    if kind != "c":
+        return None
+    fwd = G.BatchPlan("c", dims, batch, form="tc")
+    inv = G.BatchPlan("ci", dims, batch, form="tc") if with_inv else None
+    ref_r, ref_i = mid[0].clone(), mid[1].clone()
+
+    def step():
+        fwd.launch(src[0], src[1], mid[0], mid[1], stream)
+        if inv:
+            inv.launch(mid[0], mid[1], back[0], back[1], stream)
+    for _ in range(3):
+        step()
+    torch.cuda.synchronize()
+    n = int(np.prod(dims))
+    rows = min(batch, 64) * n
+    num = ((mid[0][:rows] - ref_r[:rows]) ** 2 + (mid[1][:rows] - ref_i[:rows]) ** 2).sum().item()
+    den = (ref_r[:rows] ** 2 + ref_i[:rows] ** 2).sum().item()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    steps = 20
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    return {"value": round(per_step_flops / (ms / 1e3) / 1e9, 2), "unit": "GFLOP/s", "ms_per_step": round(ms, 4),
+            "ratio_to_plain": round(plain_ms / ms, 3), "rel_l2_vs_plain_fp32": float("%.3g" % ((num / den) ** 0.5)),
+            "launches_per_step": fwd.launches + (inv.launches if inv else 0),
+            "note": "tcgen05 DFT-16 stages, FP16 hi+lo operands, FP32 accumulation in TMEM; "
+                    "tensor-pipe utilisation in profiles/line_fft_256_cols_tc_c4.md"}
 
 
 def e2e_rate(args, kind, dims, batch, src, G, torch, world):
@@ -468,6 +512,7 @@ def main():
     ap.add_argument("--form", default="plain", choices=["plain", "tc"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-tc", action="store_true", help="skip timing the tensor-core form beside the plain one")
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--soak", type=float, default=1.5, help="seconds of untimed load before the timed region")
     ap.add_argument("--traffic", type=float, default=None,

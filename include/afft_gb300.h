@@ -206,6 +206,12 @@ AFFT_GB300_API int afft_gb300_release(void* plan);
 AFFT_GB300_API size_t afft_gb300_plan_describe(int kind, size_t ndim,
   const size_t* dim, size_t batch, int format, char* buf, size_t buflen);
 
+/* Self-test of the library's bounded device waits (no counterpart in afft):
+ * launches a kernel that waits on a barrier nothing releases, for `iters`
+ * polls, and returns AFFT_GB300_ETIMEOUT when the kernel gave up and
+ * reported it as designed (-1 on a CUDA error).  Nothing faults or hangs. */
+AFFT_GB300_API int afft_gb300_selftest_bounded_wait(int iters);
+
 /* Number of this library's kernel launches one transform of `plan` issues. */
 AFFT_GB300_API int afft_gb300_plan_launches(const void* plan);
 
