@@ -166,7 +166,10 @@ static void* create_impl(int kind, size_t ndim, const size_t* dim, size_t batch,
     set_error(AFFT_GB300_ENOMEM, "scratch allocation failed");
     return nullptr;
   }
-  if (cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking) != cudaSuccess) {
+  // A blocking stream: the synchronous transform calls are ordered after
+  // work the caller queued on the default stream (the input is complete),
+  // as afft's synchronous calls read finished data.
+  if (cudaStreamCreateWithFlags(&P->stream, cudaStreamDefault) != cudaSuccess) {
     cudaGetLastError();
     set_error(AFFT_GB300_ECUDA, "stream creation failed");
     return nullptr;
@@ -269,8 +272,8 @@ static int transform_sync(void* plan, const float* sr, const float* si, float* d
       if (!P->chunk) k = 1;
     }
     P->nchunks = k;
-    if (cudaStreamCreateWithFlags(&P->copy_in, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&P->copy_out, cudaStreamNonBlocking) != cudaSuccess) {
+    if (cudaStreamCreateWithFlags(&P->copy_in, cudaStreamDefault) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&P->copy_out, cudaStreamDefault) != cudaSuccess) {
       cudaGetLastError();
       set_error(AFFT_GB300_ECUDA, "stream creation failed");
       return AFFT_GB300_ECUDA;

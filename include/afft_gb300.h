@@ -18,8 +18,9 @@
  *    dst_im each hold (d0/2+1)*prod(dims[1:]) values); real inverse reads
  *    that layout, using only the real part of planes 0 and d0/2;
  *  - the caller owns `mem` (size from *_memsize) and every data array; a plan
- *    is placement-built into `mem`; transform calls are synchronous: dst is
- *    complete when the call returns.
+ *    is placement-built into `mem`; transform calls are synchronous: they run
+ *    after work already queued on the CUDA default stream (so device inputs
+ *    produced there are complete) and dst is complete when the call returns.
  *
  * Where the data lives: transform accepts device pointers (cudaMalloc,
  * managed) and host pointers (pageable or pinned).  Host data is staged
