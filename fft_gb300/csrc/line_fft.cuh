@@ -33,6 +33,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "tc_dft.cuh"
 
 namespace agb {
@@ -52,9 +54,11 @@ struct LineParams {
   LineIO in, out;
   long long nlines;         // lines to transform
   const float2* tw;         // stage twiddles for this L
-  // four-step twiddle W_N^{((q >> tw_qshift) & tw_qmask) * k}: N = tw_n
-  // (0 = none),
+  // four-step twiddle W_N^{t2 k}, t2 = (q >> tw_qshift) & tw_qmask, N = tw_n
+  // (0 = none): tw_full[t2 * L + k] (L: the line length) when tw_full is
+  // set, else
   // W_N^m = tw_hi[m >> tw_lo_bits] * tw_lo[m & ((1 << tw_lo_bits) - 1)]
+  const float2* tw_full;
   const float2* tw_hi;
   const float2* tw_lo;
   long long tw_n;
@@ -280,11 +284,19 @@ __device__ __forceinline__ void run_stages(float2 (&v)[Sched<LOGL>::E], int t, i
   }
 }
 
+// t2 < 2^11 and k < 2^11, so t2 * k fits 32 bits; L is the line length.
+// FULL: read the matrix table tw_full, else the hi/lo pair.
+template <int L, bool FULL>
 __device__ __forceinline__ float2 fourstep_twiddle(const LineParams& p, long long q, int k) {
-  long long m = (((q >> p.tw_qshift) & p.tw_qmask) * (long long)k) & (p.tw_n - 1);
-  float2 a = ldg2(p.tw_hi + (m >> p.tw_lo_bits));
-  float2 b = ldg2(p.tw_lo + (m & ((1LL << p.tw_lo_bits) - 1)));
-  return cmul(a, b);
+  const int t2 = (int)((q >> p.tw_qshift) & p.tw_qmask);
+  if constexpr (FULL) {
+    return ldg2(p.tw_full + t2 * L + k);
+  } else {
+    const int m = (t2 * k) & ((int)p.tw_n - 1);
+    float2 a = ldg2(p.tw_hi + (m >> p.tw_lo_bits));
+    float2 b = ldg2(p.tw_lo + (m & ((1 << p.tw_lo_bits) - 1)));
+    return cmul(a, b);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -377,16 +389,10 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
   run_stages<LOGL, C, COLS, WARP_ONLY, 0, TC>(v, t, c, p.tw, sm, ts);
 
   if constexpr (KIND == LK_C2C) {
-    if (p.tw_n) {
-#pragma unroll
-      for (int e = 0; e < E; e++) v[e] = cmul(v[e], fourstep_twiddle(p, q, t + T * e));
-    }
-    if (p.inverse) {
-#pragma unroll
-      for (int e = 0; e < E; e++) v[e] = cswap(v[e]);
-    }
     if constexpr (TSTORE) {
-      // computed with the cols mapping, stored with the rows mapping
+      // computed with the cols mapping, stored with the rows mapping; the
+      // four-step twiddle is applied here, where consecutive threads walk
+      // along one line (coalesced table reads, no values held across it)
       if constexpr (Sc::NSTAGES > 1) line_sync<false>();
 #pragma unroll
       for (int e = 0; e < E; e++) sm.put(c, t + T * e, v[e]);
@@ -395,30 +401,57 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
       const long long q2 = cta * C + c2;
       if (q2 < p.nlines) {
         const long long base = line_off(p.out, q2);
+        const bool inv = p.inverse;
+        // one branch-free loop per case, so the twiddle loads issue together
+        // tw: 0 none, 1 matrix table, 2 hi/lo pair
+        auto emit = [&](auto tw) {
+          constexpr int TW = decltype(tw)::value;
 #pragma unroll
-        for (int e = 0; e < E; e++) {
-          const float2 x = sm.get(c2, t2 + T * e);
-          const long long a = base + (long long)(t2 + T * e) * p.out.es;
-          p.out.re[a] = x.x;
-          p.out.im[a] = x.y;
+          for (int e = 0; e < E; e++) {
+            float2 x = sm.get(c2, t2 + T * e);
+            if constexpr (TW) x = cmul(x, fourstep_twiddle<L, TW == 1>(p, q2, t2 + T * e));
+            x = inv ? cswap(x) : x;
+            const long long a = base + (long long)(t2 + T * e) * p.out.es;
+            p.out.re[a] = x.x;
+            p.out.im[a] = x.y;
+          }
+        };
+        if (!p.tw_n) emit(std::integral_constant<int, 0>{});
+        else if (p.tw_full) emit(std::integral_constant<int, 1>{});
+        else emit(std::integral_constant<int, 2>{});
+      }
+    } else {
+      // four-step twiddles only occur in cols passes
+      if constexpr (COLS) {
+        if (p.tw_n && p.tw_full) {
+#pragma unroll
+          for (int e = 0; e < E; e++) v[e] = cmul(v[e], fourstep_twiddle<L, true>(p, q, t + T * e));
+        } else if (p.tw_n) {
+#pragma unroll
+          for (int e = 0; e < E; e++) v[e] = cmul(v[e], fourstep_twiddle<L, false>(p, q, t + T * e));
         }
       }
-    } else if (active) {
-      const long long base = line_off(p.out, q);
-      if constexpr (UNIT) {
-        float* pr = p.out.re + base + t;
-        float* pi = p.out.im + base + t;
+      if (p.inverse) {
 #pragma unroll
-        for (int e = 0; e < E; e++) {
-          pr[T * e] = v[e].x;
-          pi[T * e] = v[e].y;
-        }
-      } else {
+        for (int e = 0; e < E; e++) v[e] = cswap(v[e]);
+      }
+      if (active) {
+        const long long base = line_off(p.out, q);
+        if constexpr (UNIT) {
+          float* pr = p.out.re + base + t;
+          float* pi = p.out.im + base + t;
 #pragma unroll
-        for (int e = 0; e < E; e++) {
-          const long long a = base + (long long)(t + T * e) * p.out.es;
-          p.out.re[a] = v[e].x;
-          p.out.im[a] = v[e].y;
+          for (int e = 0; e < E; e++) {
+            pr[T * e] = v[e].x;
+            pi[T * e] = v[e].y;
+          }
+        } else {
+#pragma unroll
+          for (int e = 0; e < E; e++) {
+            const long long a = base + (long long)(t + T * e) * p.out.es;
+            p.out.re[a] = v[e].x;
+            p.out.im[a] = v[e].y;
+          }
         }
       }
     }

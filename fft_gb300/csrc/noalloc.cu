@@ -155,6 +155,7 @@ extern "C" int afft_gb300_c2c_noalloc(const float* src_re, const float* src_im, 
     p.out = noalloc_bind(op.out, base);
     p.tw = D->stage + D->stage_off[op.k.logl];
     if (p.tw_n) {
+      p.tw_full = nullptr;   // the static tables are the hi/lo pair
       p.tw_hi = D->hi + (size_t)(lN - kNoallocMinLog) * 2048;
       p.tw_lo = D->lo + (size_t)(lN - kNoallocMinLog) * 2048;
       p.tw_lo_bits = D->lo_bits[lN];

@@ -77,25 +77,33 @@ static float2 root_f(long long m, long long N) {
 
 struct TableCache {
   std::mutex mu;
-  std::map<std::pair<int, long long>, float2*> tables;  // (device*4 + type, key)
+  std::map<std::pair<int, long long>, float2*> tables;  // (device * 8 + type, key)
 };
 static TableCache& tcache() {
   static TableCache* c = new TableCache();  // never destroyed: outlives static plans
   return *c;
 }
 
-static const float2* upload(int type, long long key, const std::vector<float2>& host) {
+// Device copy of table (type, key) on the current device; `make` builds the
+// host table on the first request only.
+template <class F>
+static const float2* cached_table(int type, long long key, F make) {
   int dev = 0;
   cudaGetDevice(&dev);
   auto& C = tcache();
   std::lock_guard<std::mutex> g(C.mu);
-  auto id = std::make_pair(dev * 4 + type, key);
+  auto id = std::make_pair(dev * 8 + type, key);
   auto it = C.tables.find(id);
   if (it != C.tables.end()) return it->second;
+  const std::vector<float2> host = make();
   float2* d = nullptr;
   size_t bytes = std::max<size_t>(host.size(), 1) * sizeof(float2);
   if (cudaMalloc(&d, bytes) != cudaSuccess) return nullptr;
-  if (!host.empty()) cudaMemcpy(d, host.data(), host.size() * sizeof(float2), cudaMemcpyHostToDevice);
+  if (!host.empty() &&
+      cudaMemcpy(d, host.data(), host.size() * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaFree(d);
+    return nullptr;
+  }
   C.tables[id] = d;
   return d;
 }
@@ -139,13 +147,15 @@ void fourstep_table_host(long long N, std::vector<float2>* hi, std::vector<float
 }
 
 const float2* stage_twiddles(int logl) {
-  return upload(0, logl, stage_table_dispatch(logl, std::make_integer_sequence<int, 15>{}));
+  return cached_table(0, logl, [&] { return stage_table_dispatch(logl, std::make_integer_sequence<int, 15>{}); });
 }
 
 const float2* real_twiddles(long long L) {
-  std::vector<float2> t(L);
-  for (long long k = 0; k < L; k++) t[k] = root_f(k, 2 * L);
-  return upload(1, L, t);
+  return cached_table(1, L, [&] {
+    std::vector<float2> t(L);
+    for (long long k = 0; k < L; k++) t[k] = root_f(k, 2 * L);
+    return t;
+  });
 }
 
 // The real 32x32 DFT-16 matrix M = [[Wr, Wi], [-Wi, Wr]] of the TC form,
@@ -199,13 +209,33 @@ int* tc_error_word() {
 void fourstep_tables(long long N, const float2** hi, const float2** lo, int* lo_bits) {
   int lb = 0;
   while ((1LL << (2 * lb)) < N) lb++;  // lo covers about sqrt(N) entries
-  long long nlo = 1LL << lb, nhi = (N + nlo - 1) / nlo;
-  std::vector<float2> th(nhi), tl(nlo);
-  for (long long j = 0; j < nhi; j++) th[j] = root_f(j * nlo, N);
-  for (long long j = 0; j < nlo; j++) tl[j] = root_f(j, N);
-  *hi = upload(2, N, th);
-  *lo = upload(3, N, tl);
+  const long long nlo = 1LL << lb, nhi = (N + nlo - 1) / nlo;
+  *hi = cached_table(2, N, [&] {
+    std::vector<float2> th(nhi);
+    for (long long j = 0; j < nhi; j++) th[j] = root_f(j * nlo, N);
+    return th;
+  });
+  *lo = cached_table(3, N, [&] {
+    std::vector<float2> tl(nlo);
+    for (long long j = 0; j < nlo; j++) tl[j] = root_f(j, N);
+    return tl;
+  });
   *lo_bits = lb;
+}
+
+std::vector<float2> fourstep_full_table_host(long long N, long long L2) {
+  const long long L1 = N / L2;
+  std::vector<float2> t(N);
+  for (long long j = 0; j < L2; j++)
+    for (long long k = 0; k < L1; k++) t[j * L1 + k] = root_f(j * k, N);
+  return t;
+}
+
+const float2* fourstep_full_table(long long N, long long L2) {
+  if (N > kFullTableMax) return nullptr;
+  int l2 = 0;
+  while ((1LL << l2) < L2) l2++;
+  return cached_table(4, (N << 6) | l2, [&] { return fourstep_full_table_host(N, L2); });
 }
 
 // ---------------------------------------------------------------------------
@@ -274,6 +304,10 @@ struct Builder {
             long long nlines, bool inverse, long long tw_n = 0, long long tw_qmask = 0,
             int tw_qshift = 0, long long real_L = 0) {
     if (!ok) return;
+    if (tw_n && !cols) {
+      fail("four-step twiddles need a cols pass");
+      return;
+    }
     Op op;
     op.type = OP_LINE;
     bool tc = P.form == FORM_TC && kind == LK_C2C && get_tc_kernel(logl, cols, tstore, &op.k);
@@ -301,7 +335,10 @@ struct Builder {
         return;
       }
       op.p.tw = stage_twiddles(logl);
-      if (tw_n) fourstep_tables(tw_n, &op.p.tw_hi, &op.p.tw_lo, &op.p.tw_lo_bits);
+      if (tw_n) {
+        fourstep_tables(tw_n, &op.p.tw_hi, &op.p.tw_lo, &op.p.tw_lo_bits);
+        op.p.tw_full = fourstep_full_table(tw_n, tw_qmask + 1);
+      }
       if (real_L) op.p.rtw = real_twiddles(real_L);
       if (tc) {
         op.p.tc_b = tc_matrix_table();
@@ -315,7 +352,8 @@ struct Builder {
     op.grid = (nlines + op.k.lines_per_cta - 1) / op.k.lines_per_cta;
     op.threads = op.k.threads;
     op.smem = op.k.smem;
-    if (!dry && (!op.p.tw || (tw_n && (!op.p.tw_hi || !op.p.tw_lo)) || (real_L && !op.p.rtw))) {
+    if (!dry && (!op.p.tw || (tw_n && (!op.p.tw_hi || !op.p.tw_lo)) ||
+                 (tw_n && tw_n <= kFullTableMax && !op.p.tw_full) || (real_L && !op.p.rtw))) {
       fail("twiddle table allocation failed");
       return;
     }

@@ -106,6 +106,11 @@ int validate_shape(int ndim, const size_t* dim, int* ndim_out, long long* dims_o
 const float2* stage_twiddles(int logl);
 const float2* real_twiddles(long long L);         // W_{2L}^k, k < L
 void fourstep_tables(long long N, const float2** hi, const float2** lo, int* lo_bits);
+// The four-step twiddle as one matrix, W_N^{t2 k} at [t2 * L1 + k], for
+// N <= kFullTableMax (nullptr above): one coalesced load per element.
+constexpr long long kFullTableMax = 1LL << 20;
+const float2* fourstep_full_table(long long N, long long L2);
+std::vector<float2> fourstep_full_table_host(long long N, long long L2);
 // The same tables on the host, without touching the device.
 std::vector<float2> stage_table_host(int logl);
 void fourstep_table_host(long long N, std::vector<float2>* hi, std::vector<float2>* lo, int* lo_bits);

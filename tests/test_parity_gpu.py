@@ -166,6 +166,16 @@ def test_1d_all_sizes(kind, n, dev):
     check(kind, [n], a, b, run_plan(kind, [n], a, b, dev))
 
 
+@pytest.mark.parametrize("kind,n", [("c", 1 << 21), ("ci", 1 << 21), ("c", 1 << 22), ("ci", 1 << 22),
+                                    ("r", 1 << 21), ("ri", 1 << 22), ("r", 1 << 23), ("ri", 1 << 23)])
+def test_1d_longest_axes(kind, n, dev):
+    # complex axes above 2^20 points take the two-table four-step twiddle,
+    # those up to 2^20 the single-matrix one; 2^22 complex points is the
+    # longest axis
+    a, b = inputs(kind, [n], 7)
+    check(kind, [n], a, b, run_plan(kind, [n], a, b, dev))
+
+
 ND = [[2, 2], [4, 64], [64, 4], [256, 256], [32, 4096], [4096, 32], [8, 16384], [16384, 8], [4, 65536],
       [8192, 4], [16384, 16, 2], [2, 2, 2], [16, 32, 64], [64, 64, 64], [8, 2048, 8], [4, 4, 4, 4, 4],
       [2, 8, 2, 8, 2, 8], [1, 512, 1, 16], [2048, 16]]
