@@ -176,6 +176,61 @@ def test_1d_longest_axes(kind, n, dev):
     check(kind, [n], a, b, run_plan(kind, [n], a, b, dev))
 
 
+def run_batch(kind, dims, batch, a, b, fmt=G.afft_split, inplace=False):
+    """A batched transform through BatchPlan on device tensors (complex
+    kinds only); returns numpy re, im."""
+    n = int(np.prod(dims))
+    p = G.BatchPlan(kind, dims, batch, fmt=fmt)
+    if fmt == G.afft_interleaved:
+        src = np.empty(2 * n * batch, np.float32)
+        src[0::2], src[1::2] = a, b
+        s = torch.from_numpy(src).cuda()
+        d = s if inplace else torch.zeros_like(s)
+        p.launch(s, None, d, None)
+        torch.cuda.synchronize()
+        o = d.cpu().numpy()
+        return o[0::2].copy(), o[1::2].copy()
+    sr, si = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
+    dr, di = (sr, si) if inplace else (torch.zeros_like(sr), torch.zeros_like(si))
+    p.launch(sr, si, dr, di)
+    torch.cuda.synchronize()
+    return dr.cpu().numpy(), di.cpu().numpy()
+
+
+# Batched two-pass shapes (four-step transforms of 2^15 and 2^16 points, and
+# 256 x 256 slices of N-D transforms) in every layout: small batches, large
+# ones, and batches that are not a multiple of the grid's resident CTAs.
+PLANE = [("c", [65536], 1), ("ci", [65536], 3), ("c", [65536], 301), ("ci", [32768], 2), ("c", [32768], 257),
+         ("c", [256, 256], 1), ("ci", [256, 256], 5), ("c", [8, 256, 256], 1), ("ci", [256, 256, 256], 1),
+         ("c", [256, 256], 97)]
+
+
+@pytest.mark.parametrize("kind,dims,batch", PLANE, ids=lambda v: str(v))
+@pytest.mark.parametrize("fmt", [G.afft_split, G.afft_interleaved], ids=["split", "inter"])
+@pytest.mark.parametrize("inplace", [False, True], ids=["oop", "inplace"])
+def test_two_pass_batches(kind, dims, batch, fmt, inplace, dev):
+    n = int(np.prod(dims))
+    rng = np.random.default_rng(n + batch)
+    a = rng.uniform(-1, 1, n * batch).astype(np.float32)
+    b = rng.uniform(-1, 1, n * batch).astype(np.float32)
+    gr, gi = run_batch(kind, dims, batch, a, b, fmt, inplace)
+    # every transform of the batch against the FP64 oracle (a sample of them
+    # for the large batches)
+    idx = range(batch) if batch <= 8 else sorted({0, 1, batch // 2, batch - 2, batch - 1})
+    for t in idx:
+        sl = slice(t * n, (t + 1) * n)
+        ref = O.oracle64(kind, dims, a[sl], b[sl])
+        assert O.rel_l2((gr[sl], gi[sl]), ref) <= TOL, (kind, dims, batch, t)
+
+
+@pytest.mark.parametrize("kind", ["r", "ri"])
+@pytest.mark.parametrize("dims", [[4, 256, 256], [2, 2, 256, 256]], ids=str)
+def test_two_pass_real_slices(kind, dims, dev):
+    # 256 x 256 complex slices after (before) the halved dim-0 pass
+    a, b = inputs(kind, dims, 13)
+    check(kind, dims, a, b, run_plan(kind, dims, a, b, dev))
+
+
 ND = [[2, 2], [4, 64], [64, 4], [256, 256], [32, 4096], [4096, 32], [8, 16384], [16384, 8], [4, 65536],
       [8192, 4], [16384, 16, 2], [2, 2, 2], [16, 32, 64], [64, 64, 64], [8, 2048, 8], [4, 4, 4, 4, 4],
       [2, 8, 2, 8, 2, 8], [1, 512, 1, 16], [2048, 16]]
