@@ -1,5 +1,5 @@
 // cols-mode real line FFT instantiations (N-D real, first dim halved),
-// L = 2^0 .. 2^11
+// L = 2^0 .. 2^11; the 2048-point R2C pass is the two-CTA split form
 #include "kernels.h"
 namespace agb {
 bool get_cols_real(int logl, int kind, LineKernel* out) {
@@ -16,7 +16,9 @@ bool get_cols_real(int logl, int kind, LineKernel* out) {
       case 8: *out = make_line_kernel<8, true, LK_R2C, false>(); return true;
       case 9: *out = make_line_kernel<9, true, LK_R2C, false>(); return true;
       case 10: *out = make_line_kernel<10, true, LK_R2C, false>(); return true;
-      case 11: *out = make_line_kernel<11, true, LK_R2C, false>(); return true;
+      // 2048 points: split over two CTAs of 1024-point stages (2 CTAs/SM
+      // instead of one)
+      case 11: *out = make_line_kernel<10, true, LK_R2C_HALF, false>(); return true;
     }
   } else if (kind == LK_C2R) {
     switch (logl) {

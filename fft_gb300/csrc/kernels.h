@@ -20,6 +20,8 @@ struct LineKernel {
   int lines_per_cta;   // C
   int threads;         // T * C
   size_t smem;         // bytes of dynamic shared memory
+  int halves;          // CTAs per tile of C lines (2: the split R2C pass)
+  int stage_logl;      // log2 length of the stage twiddle table the kernel reads
 };
 
 constexpr int ROWS_MAX_LOG = 14;   // rows mode: one CTA up to 16384 points
@@ -51,24 +53,36 @@ constexpr int lines_per_cta() {
   else return T >= 256 ? 1 : 256 / T;
 }
 
+#ifndef AFFT_HALF_C
+#define AFFT_HALF_C 8
+#endif
+// lines per CTA of the split R2C pass
+template <int LOGL, bool COLS, int KIND>
+constexpr int lines_per_cta_k() {
+  return KIND == LK_R2C_HALF ? AFFT_HALF_C : lines_per_cta<LOGL, COLS>();
+}
+
 template <int LOGL, bool COLS, int KIND, bool TSTORE, bool TC = false, bool UNIT = false>
 LineKernel make_line_kernel() {
-  constexpr int C = lines_per_cta<LOGL, COLS>();
+  constexpr int C = lines_per_cta_k<LOGL, COLS, KIND>();
   constexpr int L = 1 << LOGL;
-  static_assert(!TC || (size_t)Smem<L, C, COLS>::FLOAT2S * 8 >= (size_t)(Sched<LOGL>::T * C / 128) * 16384,
+  static_assert(!TC || (size_t)LineSmem<LOGL, C, COLS, TSTORE, TC>::FLOAT2S * 8 >= (size_t)(Sched<LOGL>::T * C / 128) * 16384,
                 "TC operand tiles must fit in the exchange buffer");
   LineKernel k;
   k.fn = &line_fft<LOGL, C, COLS, KIND, TSTORE, TC, UNIT>;
   k.grouped = &line_fft_grouped<LOGL, C, COLS, KIND, TSTORE, TC, UNIT>;
   k.tc = TC;
   k.unit = UNIT;
-  k.logl = LOGL;
+  // the split R2C pass transforms lines of 2^(LOGL+1) points with stages of 2^LOGL
+  k.logl = KIND == LK_R2C_HALF ? LOGL + 1 : LOGL;
   k.cols = COLS;
-  k.kind = KIND;
+  k.kind = KIND == LK_R2C_HALF ? LK_R2C : KIND;
+  k.halves = KIND == LK_R2C_HALF ? 2 : 1;
+  k.stage_logl = LOGL;
   k.tstore = TSTORE;
   k.lines_per_cta = C;
   k.threads = Sched<LOGL>::T * C;
-  k.smem = (size_t)Smem<L, C, COLS>::FLOAT2S * sizeof(float2);
+  k.smem = (size_t)LineSmem<LOGL, C, COLS, TSTORE, TC>::FLOAT2S * sizeof(float2);
   return k;
 }
 

@@ -39,7 +39,8 @@
 
 namespace agb {
 
-enum LineKind { LK_C2C = 0, LK_R2C = 1, LK_C2R = 2 };
+// LK_R2C_HALF: the cols R2C pass split over two CTAs per tile (below).
+enum LineKind { LK_C2C = 0, LK_R2C = 1, LK_C2R = 2, LK_R2C_HALF = 3 };
 
 struct LineIO {
   float* re;
@@ -185,25 +186,45 @@ __device__ __forceinline__ void dft(float2 (&x)[R]) {
 }
 
 // ---------------------------------------------------------------------------
-// shared-memory layout: complex values as float2, padded so the Stockham
+// shared-memory layout: complex values as float2, arranged so the Stockham
 // scatter and the canonical gather hit distinct bank pairs per half-warp and
 // every per-element offset is a compile-time constant:
 //   rows mode: line c at c * LP, element j at j + j/16   (LP = L + L/16)
 //   cols mode: element j of line c at j * CP + c          (CP = C + 1)
+//   cols mode, SWAP = k >= 0 (8 lines): element j of line c at
+//              (j ^ bit_k(j >> 1)) * 8 + c, unpadded.  A half-warp then
+//              touches two rows; the padded layout puts both in the same
+//              bank half for the strided scatter of the stages (2-way
+//              conflicts), while swapping the rows of a pair keyed on bit
+//              k = log2(first radix / 2) of the pair index separates them for
+//              the scatter and the gather at every length (checked by an
+//              exhaustive bank count over all stages and warps).
 // ---------------------------------------------------------------------------
-template <int L, int C, bool COLS>
+template <int L, int C, bool COLS, int SWAP = -1>
 struct Smem {
+  static_assert(SWAP < 0 || (COLS && C == 8), "row-pair swap layout: cols mode, 8 lines");
   static constexpr int LP = L + L / 16;
-  static constexpr int CP = C + 1;
+  static constexpr int CP = SWAP >= 0 ? C : C + 1;
   static constexpr int FLOAT2S = COLS ? L * CP : C * LP;
   float2* s;
   __device__ __forceinline__ int idx(int c, int j) const {
-    if constexpr (COLS) return j * CP + c;
+    if constexpr (COLS && SWAP >= 0) return (j ^ ((j >> (SWAP + 1)) & 1)) * C + c;
+    else if constexpr (COLS) return j * CP + c;
     else return c * LP + j + (j >> 4);
   }
   __device__ __forceinline__ void put(int c, int j, float2 v) const { s[idx(c, j)] = v; }
   __device__ __forceinline__ float2 get(int c, int j) const { return s[idx(c, j)]; }
 };
+
+// The layout a line kernel uses: the row-pair swap for 8-line cols tiles
+// whose exchange is only read in the cols mapping (not the transposing store,
+// which reads along lines, nor the TC operand tiles).
+template <int LOGL>
+constexpr int swap_bit() {
+  return LOGL % 4 == 0 ? 3 : LOGL % 4 - 1;
+}
+template <int LOGL, int C, bool COLS, bool TSTORE, bool TC>
+using LineSmem = Smem<(1 << LOGL), C, COLS, (COLS && C == 8 && !TSTORE && !TC && LOGL >= 8) ? swap_bit<LOGL>() : -1>;
 
 template <bool WARP_ONLY>
 __device__ __forceinline__ void line_sync() {
@@ -256,9 +277,9 @@ __device__ __forceinline__ void stage(float2 (&v)[E], int t, int c, const float2
 
 // All stages; v holds the input in canonical layout on entry and the output
 // in canonical layout on exit.
-template <int LOGL, int C, bool COLS, bool WARP_ONLY, int S, bool TC = false>
+template <int LOGL, int C, bool COLS, bool WARP_ONLY, int S, bool TC = false, class SM>
 __device__ __forceinline__ void run_stages(float2 (&v)[Sched<LOGL>::E], int t, int c, const float2* tw,
-                                           const Smem<Sched<LOGL>::L, C, COLS>& sm, TcState* ts = nullptr) {
+                                           const SM& sm, TcState* ts = nullptr) {
   using Sc = Sched<LOGL>;
   constexpr int E = Sc::E, T = Sc::T;
   constexpr int NT = (Sc::T * C) / 128;
@@ -313,17 +334,99 @@ constexpr int min_ctas() {
   return AFFT_REG_CAP ? (65536 / (AFFT_REG_CAP * NT) > 0 ? 65536 / (AFFT_REG_CAP * NT) : 1) : 1;
 }
 
+// The real forward (R2C) pass along a strided axis of Z = 2 Lh complex
+// points (Lh = 2^LOGL), split over two CTAs per tile of C lines.  With the
+// first radix-2 step of a decimation in frequency,
+//   a[j] = z[j] + z[j + Lh],  b[j] = (z[j] - z[j + Lh]) W_{2Lh}^j,
+// FFT_Lh(a) gives the even bins Z[2m] and FFT_Lh(b) the odd bins Z[2m+1].
+// CTA half h = cta & 1 computes one of them, so it needs the exchange buffer
+// of Lh points per line, not 2 Lh: twice the CTAs fit on an SM.  The real
+// post-pass pairs bin k with 2 Lh - k, which has the same parity, so both
+// halves finish on their own: h = 0 pairs m with Lh - m (mod Lh), h = 1 pairs
+// m with Lh - 1 - m.  Both CTAs of a tile read the whole tile (the second
+// read is served by L2).  rtw = W_{4Lh}^k, k < 2 Lh, as for the unsplit pass;
+// W_{2Lh}^j = rtw[2j].  The stage twiddles are those of Lh.
+template <int LOGL, int C>
+__device__ __forceinline__ void r2c_half_body(const LineParams& p, long long cta) {
+  using Sc = Sched<LOGL>;
+  constexpr int Lh = Sc::L, E = Sc::E, T = Sc::T, L = 2 * Lh;
+  constexpr bool WARP_ONLY = T * C <= 32;
+  extern __shared__ __align__(1024) float2 smem_raw[];
+  LineSmem<LOGL, C, true, false, false> sm{smem_raw};
+  const int tid = threadIdx.x;
+  const int c = tid % C, t = tid / C;
+  const int h = (int)(cta & 1);
+  const long long q = (cta >> 1) * C + c;
+  const bool active = q < p.nlines;
+
+  float2 v[E];
+  if (active) {
+    const long long base = line_off(p.in, q);
+    const long long half = (long long)Lh * p.in.es;
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+      const int j = t + T * e;
+      const long long a0 = base + (long long)j * p.in.es;
+      const float2 x0 = make_float2(__ldg(p.in.re + a0), __ldg(p.in.im + a0));
+      const float2 x1 = make_float2(__ldg(p.in.re + a0 + half), __ldg(p.in.im + a0 + half));
+      v[e] = h ? cmul(csub(x0, x1), ldg2(p.rtw + 2 * j)) : cadd(x0, x1);
+    }
+  } else {
+#pragma unroll
+    for (int e = 0; e < E; e++) v[e] = make_float2(0.f, 0.f);
+  }
+
+  run_stages<LOGL, C, true, WARP_ONLY, 0>(v, t, c, p.tw, sm);
+
+  // real forward post-pass on this half's bins (the formula of the unsplit
+  // pass below: X[k] = a - i b, X[0] and X[L] from Z[0])
+  if constexpr (Sc::NSTAGES > 1) line_sync<WARP_ONLY>();
+#pragma unroll
+  for (int e = 0; e < E; e++) sm.put(c, t + T * e, v[e]);
+  line_sync<WARP_ONLY>();
+  if (active) {
+    const long long base = line_off(p.out, q);
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+      const int m = t + T * e;
+      const int k = 2 * m + h;
+      const float2 s0 = v[e];
+      const float2 s1 = sm.get(c, h ? (Lh - 1 - m) : ((Lh - m) & (Lh - 1)));
+      float2 x;
+      if (k == 0) {
+        x = make_float2(s0.x + s0.y, 0.f);
+        const long long aL = base + (long long)L * p.out.es;
+        p.out.re[aL] = s0.x - s0.y;
+        p.out.im[aL] = 0.f;
+      } else {
+        const float2 w = ldg2(p.rtw + k);
+        const float2 a = make_float2(0.5f * (s0.x + s1.x), 0.5f * (s0.y - s1.y));
+        const float2 d = make_float2(0.5f * (s0.x - s1.x), 0.5f * (s0.y + s1.y));
+        x = cadd(a, cmul_negi(cmul(d, w)));
+      }
+      const long long a = base + (long long)k * p.out.es;
+      p.out.re[a] = x.x;
+      p.out.im[a] = x.y;
+    }
+  }
+}
+
 // The body of one CTA's work: lines [cta*C, cta*C + C) of the launch `p`.
 // UNIT: both element strides are 1 (split complex rows), so element offsets
 // are compile-time constants instead of runtime 64-bit products.
 template <int LOGL, int C, bool COLS, int KIND, bool TSTORE, bool TC = false, bool UNIT = false>
 __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta, TcState* ts = nullptr) {
+  if constexpr (KIND == LK_R2C_HALF) {
+    static_assert(COLS && !TSTORE && !TC, "the split R2C pass is a plain cols pass");
+    r2c_half_body<LOGL, C>(p, cta);
+    return;
+  }
   using Sc = Sched<LOGL>;
   constexpr int L = Sc::L, E = Sc::E, T = Sc::T;
   // a line lives inside one warp: rows mode with T <= 32, or a single line
   constexpr bool WARP_ONLY = (!COLS && T <= 32) || (T * C <= 32);
   extern __shared__ __align__(1024) float2 smem_raw[];
-  Smem<L, C, COLS> sm{smem_raw};
+  LineSmem<LOGL, C, COLS, TSTORE, TC> sm{smem_raw};
 
   const int tid = threadIdx.x;
   const int c = COLS ? (tid % C) : (tid / T);

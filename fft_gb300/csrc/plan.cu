@@ -334,7 +334,7 @@ struct Builder {
         fail("kernel shared memory configuration failed");
         return;
       }
-      op.p.tw = stage_twiddles(logl);
+      op.p.tw = stage_twiddles(op.k.stage_logl);
       if (tw_n) {
         fourstep_tables(tw_n, &op.p.tw_hi, &op.p.tw_lo, &op.p.tw_lo_bits);
         op.p.tw_full = fourstep_full_table(tw_n, tw_qmask + 1);
@@ -349,7 +349,7 @@ struct Builder {
         }
       }
     }
-    op.grid = (nlines + op.k.lines_per_cta - 1) / op.k.lines_per_cta;
+    op.grid = (nlines + op.k.lines_per_cta - 1) / op.k.lines_per_cta * op.k.halves;
     op.threads = op.k.threads;
     op.smem = op.k.smem;
     if (!dry && (!op.p.tw || (tw_n && (!op.p.tw_hi || !op.p.tw_lo)) ||
@@ -641,9 +641,11 @@ std::string describe_plan(const Plan& P) {
     if (op.type == OP_LINE) {
       snprintf(buf, sizeof buf,
                "{\"type\":\"line\",\"logl\":%d,\"cols\":%d,\"lk\":%d,\"tstore\":%d,\"tc\":%d,\"C\":%d,"
+               "\"halves\":%d,"
                "\"threads\":%d,\"smem\":%zu,\"grid\":%lld,\"nlines\":%lld,\"inverse\":%d,"
                "\"tw_n\":%lld,\"tw_qmask\":%lld,\"tw_qshift\":%d,\"real_L\":%lld,",
-               op.k.logl, op.k.cols, op.k.kind, op.k.tstore, op.k.tc, op.k.lines_per_cta, op.threads, op.smem,
+               op.k.logl, op.k.cols, op.k.kind, op.k.tstore, op.k.tc, op.k.lines_per_cta, op.k.halves, op.threads,
+               op.smem,
                op.grid, op.p.nlines, op.p.inverse, op.p.tw_n, op.p.tw_qmask, op.p.tw_qshift, op.real_L);
     } else if (op.type == OP_REAL) {
       snprintf(buf, sizeof buf,

@@ -87,7 +87,9 @@ AFFT_GB300_API afft_32_ci_type* afft_32_ci_create(
 AFFT_GB300_API void afft_32_ci_transform(afft_32_ci_type* state,
   const float* src_re, const float* src_im, float* dst_re, float* dst_im);
 
-/* Replaces fft.h:34-38 (real forward, first dimension halved). */
+/* Replaces fft.h:34-38 (real forward, first dimension halved).  Real
+ * transforms (forward and inverse) need src and dst not to overlap;
+ * complex transforms may run in place (src == dst). */
 typedef struct afft_32_r_struct afft_32_r_type;
 AFFT_GB300_API size_t afft_32_r_memsize(size_t ndim, const size_t* dim, int format, int impl);
 AFFT_GB300_API afft_32_r_type* afft_32_r_create(

@@ -110,10 +110,11 @@ def _gather(B, acc, spec, q, idx, cta):
 
 
 def _scatter(B, acc, spec, q, idx, cta, val):
+    """cta: per line, or per (line, element) when a line is split over CTAs."""
     ore = line_offsets(spec, q)[:, None] + idx[None, :] * spec["es"]
     bre, are = B.addr(spec["re"], ore)
     bim, aim = B.addr(spec["im"], ore)
-    ctas = np.broadcast_to(cta[:, None], ore.shape)
+    ctas = cta if cta.ndim == 2 else np.broadcast_to(cta[:, None], ore.shape)
     acc.note(acc.writes, bre, are, ctas)
     acc.note(acc.writes, bim, aim, ctas)
     return (bre, are, val.real), (bim, aim, val.imag)
@@ -133,7 +134,8 @@ def run_op(B, op):
     if t == "line":
         L = 1 << op["logl"]
         q = np.arange(op["nlines"], dtype=np.int64)
-        cta = q // op["C"]
+        halves = op.get("halves", 1)
+        cta = q // op["C"] * halves
         lk = op["lk"]
         if lk == 2:  # C2R: reads L+1 bins
             X = _gather(B, acc, op["in"], q, np.arange(L + 1), cta)
@@ -162,6 +164,11 @@ def run_op(B, op):
                 out = (s0 + np.conj(s1)) / 2 - 0.5j * w(k, 2 * L) * (s0 - np.conj(s1))
                 out[:, 0] = Xf[:, 0].real + Xf[:, 0].imag
                 out[:, L] = Xf[:, 0].real - Xf[:, 0].imag
+                if halves == 2:
+                    # both CTAs of a tile read the whole line; CTA h writes
+                    # the bins of parity h
+                    _gather(B, acc, op["in"], q, np.arange(L), cta + 1)
+                    cta = cta[:, None] + (k[None, :] & 1)
                 pending += _scatter(B, acc, op["out"], q, k, cta, out)
     elif t == "real":
         L = op["L"]
