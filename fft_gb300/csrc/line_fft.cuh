@@ -192,15 +192,17 @@ __device__ __forceinline__ void dft(float2 (&x)[R]) {
 //   rows mode: line c at c * LP, element j at j + j/16   (LP = L + L/16)
 //   cols mode: element j of line c at j * CP + c          (CP = C + 1)
 //   cols mode, SWAP = k >= 0 (8 lines): element j of line c at
-//              (j ^ bit_k(j >> 1)) * 8 + c, unpadded.  A half-warp then
-//              touches two rows; the padded layout puts both in the same
-//              bank half for the strided scatter of the stages (2-way
-//              conflicts), while swapping the rows of a pair keyed on bit
-//              k = log2(first radix / 2) of the pair index separates them for
-//              the scatter and the gather at every length (checked by an
-//              exhaustive bank count over all stages and warps).
+//              (j ^ bit_k(j >> 1)) * 8 + c, unpadded (XOR: c ^ ((j >> 1) & 7)).
+//              A half-warp of the cols mapping touches two rows; the padded
+//              layout puts both in the same bank half for the strided
+//              scatter of the stages (2-way conflicts).  Swapping the rows
+//              of a pair keyed on bit k = log2(first radix / 2) of the pair
+//              index separates them for the scatter and the gather.  With
+//              XOR, 16 consecutive elements of one line (the transposing
+//              store's reads) also spread over all banks.  Both checked by an
+//              exhaustive bank count over all stages and warps.
 // ---------------------------------------------------------------------------
-template <int L, int C, bool COLS, int SWAP = -1>
+template <int L, int C, bool COLS, int SWAP = -1, bool XOR = false>
 struct Smem {
   static_assert(SWAP < 0 || (COLS && C == 8), "row-pair swap layout: cols mode, 8 lines");
   static constexpr int LP = L + L / 16;
@@ -208,7 +210,8 @@ struct Smem {
   static constexpr int FLOAT2S = COLS ? L * CP : C * LP;
   float2* s;
   __device__ __forceinline__ int idx(int c, int j) const {
-    if constexpr (COLS && SWAP >= 0) return (j ^ ((j >> (SWAP + 1)) & 1)) * C + c;
+    if constexpr (COLS && SWAP >= 0 && XOR) return (j ^ ((j >> (SWAP + 1)) & 1)) * C + (c ^ ((j >> 1) & 7));
+    else if constexpr (COLS && SWAP >= 0) return (j ^ ((j >> (SWAP + 1)) & 1)) * C + c;
     else if constexpr (COLS) return j * CP + c;
     else return c * LP + j + (j >> 4);
   }
@@ -217,14 +220,14 @@ struct Smem {
 };
 
 // The layout a line kernel uses: the row-pair swap for 8-line cols tiles
-// whose exchange is only read in the cols mapping (not the transposing store,
-// which reads along lines, nor the TC operand tiles).
+// (not the TC operand tiles, which have their own layout), with the XOR when
+// the transposing store reads the buffer along lines.
 template <int LOGL>
 constexpr int swap_bit() {
   return LOGL % 4 == 0 ? 3 : LOGL % 4 - 1;
 }
 template <int LOGL, int C, bool COLS, bool TSTORE, bool TC>
-using LineSmem = Smem<(1 << LOGL), C, COLS, (COLS && C == 8 && !TSTORE && !TC && LOGL >= 8) ? swap_bit<LOGL>() : -1>;
+using LineSmem = Smem<(1 << LOGL), C, COLS, (COLS && C == 8 && !TC && LOGL >= 8) ? swap_bit<LOGL>() : -1, TSTORE>;
 
 template <bool WARP_ONLY>
 __device__ __forceinline__ void line_sync() {
