@@ -189,7 +189,12 @@ __device__ __forceinline__ void dft(float2 (&x)[R]) {
 // shared-memory layout: complex values as float2, arranged so the Stockham
 // scatter and the canonical gather hit distinct bank pairs per half-warp and
 // every per-element offset is a compile-time constant:
-//   rows mode: line c at c * LP, element j at j + j/16   (LP = L + L/16)
+//   rows mode: line c at c * LP, element j at j + j/16   (LP = L + L/16);
+//              short lines, where a warp spans 8 to 16 lines, instead:
+//              L = 128: j + j/8 (LP 152), L = 64: j + j/4 (LP 84),
+//              L = 32: j ^ (3 (c >> 2) mod 32) (LP 36), each found by an
+//              exhaustive bank count (the j/16 form costs 1.5 to 2.5 times
+//              the minimum wavefronts at these lengths)
 //   cols mode: element j of line c at j * CP + c          (CP = C + 1)
 //   cols mode, SWAP = k >= 0 (8 lines): element j of line c at
 //              (j ^ bit_k(j >> 1)) * 8 + c, unpadded (XOR: c ^ ((j >> 1) & 7)).
@@ -205,7 +210,7 @@ __device__ __forceinline__ void dft(float2 (&x)[R]) {
 template <int L, int C, bool COLS, int SWAP = -1, bool XOR = false>
 struct Smem {
   static_assert(SWAP < 0 || (COLS && C == 8), "row-pair swap layout: cols mode, 8 lines");
-  static constexpr int LP = L + L / 16;
+  static constexpr int LP = L == 32 ? 36 : (L == 64 ? 84 : (L == 128 ? 152 : L + L / 16));
   static constexpr int CP = SWAP >= 0 ? C : C + 1;
   static constexpr int FLOAT2S = COLS ? L * CP : C * LP;
   float2* s;
@@ -213,6 +218,9 @@ struct Smem {
     if constexpr (COLS && SWAP >= 0 && XOR) return (j ^ ((j >> (SWAP + 1)) & 1)) * C + (c ^ ((j >> 1) & 7));
     else if constexpr (COLS && SWAP >= 0) return (j ^ ((j >> (SWAP + 1)) & 1)) * C + c;
     else if constexpr (COLS) return j * CP + c;
+    else if constexpr (L == 32) return c * LP + (j ^ (((c >> 2) * 3) & 31));
+    else if constexpr (L == 64) return c * LP + j + (j >> 2);
+    else if constexpr (L == 128) return c * LP + j + (j >> 3);
     else return c * LP + j + (j >> 4);
   }
   __device__ __forceinline__ void put(int c, int j, float2 v) const { s[idx(c, j)] = v; }
