@@ -40,7 +40,9 @@
 namespace agb {
 
 // LK_R2C_HALF: the cols R2C pass split over two CTAs per tile (below).
-enum LineKind { LK_C2C = 0, LK_R2C = 1, LK_C2R = 2, LK_R2C_HALF = 3 };
+// LK_R2C_PAIRED: pass B of a long 1D real forward with the real post-pass,
+// over tiles of mirrored column pairs (below).
+enum LineKind { LK_C2C = 0, LK_R2C = 1, LK_C2R = 2, LK_R2C_HALF = 3, LK_R2C_PAIRED = 4 };
 
 struct LineIO {
   float* re;
@@ -67,6 +69,7 @@ struct LineParams {
   int tw_qshift;
   int tw_lo_bits;
   const float2* rtw;        // real pass twiddles W_{2L}^k, k < L
+  long long pcols;          // LK_R2C_PAIRED: columns L1 of the four-step (lines per transform)
   int inverse;              // swap re/im on load and store
   const __half* tc_b;       // TC form: Mh then Ml, 32x32 FP16 each, [n][k]
   int* err;                 // TC form: error word set when a bounded wait gives up
@@ -422,6 +425,82 @@ __device__ __forceinline__ void r2c_half_body(const LineParams& p, long long cta
   }
 }
 
+// Pass B of the four-step transform of a long 1D real forward (n/2 = L =
+// L1 L2 complex points of the interleaved view) with the real post-pass
+// (onedim.hpp:1058-1108) fused in.  Pass B line (o, k1) holds Z[k1 + L1 k2]
+// for k2 < L2; the post-pass pairs Z[k] with Z[L - k], and for k1 > 0 that
+// is element L2 - 1 - k2 of column L1 - k1 (column 0 pairs with itself,
+// element (L2 - k2) mod L2).  So a CTA takes C/2 columns a .. a + C/2 - 1
+// (slots 0 .. C/2-1, a = tile C/2) and their mirrors L1 - a - m (slots
+// C/2 + m); in tile 0 the slot of the mirror "L1" holds column L1/2, which
+// pairs with itself.  After the FFTs every element yields its own bin X[k]
+// (k = k1 + L1 k2, written where the unfused pass B would write Z[k]), and
+// the column-0 thread of k2 = 0 also writes X[L] (element L2 of line
+// (o, 0)).  Lines come in whole tiles: L1 is a multiple of C.
+template <int LOGL, int C>
+__device__ __forceinline__ void r2c_paired_body(const LineParams& p, long long cta) {
+  using Sc = Sched<LOGL>;
+  constexpr int L2 = Sc::L, E = Sc::E, T = Sc::T, H = C / 2;
+  static_assert(C % 2 == 0 && T * C > 32, "paired tiles: even C, CTA-wide exchange");
+  extern __shared__ __align__(1024) float2 smem_raw[];
+  LineSmem<LOGL, C, true, false, false> sm{smem_raw};
+  const int tid = threadIdx.x;
+  const int c = tid % C, t = tid / C;
+  const long long L1 = p.pcols, tiles = L1 / C;
+  const long long o = cta / tiles, a = (cta % tiles) * H;
+  // this slot's column and its partner slot
+  long long k1;
+  int cp;
+  if (c < H) {
+    k1 = a + c;
+    cp = (a == 0 && c == 0) ? 0 : c + H;
+  } else {
+    const int m = c - H;
+    k1 = (a == 0 && m == 0) ? L1 / 2 : L1 - a - m;
+    cp = (a == 0 && m == 0) ? c : m;
+  }
+  const long long q = o * L1 + k1;
+
+  float2 v[E];
+  {
+    const long long base = line_off(p.in, q);
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+      const long long ad = base + (long long)(t + T * e) * p.in.es;
+      v[e] = make_float2(__ldg(p.in.re + ad), __ldg(p.in.im + ad));
+    }
+  }
+  run_stages<LOGL, C, true, false, 0>(v, t, c, p.tw, sm);
+
+  if constexpr (Sc::NSTAGES > 1) __syncthreads();
+#pragma unroll
+  for (int e = 0; e < E; e++) sm.put(c, t + T * e, v[e]);
+  __syncthreads();
+  const long long base = line_off(p.out, q);
+#pragma unroll
+  for (int e = 0; e < E; e++) {
+    const int k2 = t + T * e;
+    const long long k = k1 + L1 * k2;
+    const float2 s0 = v[e];
+    const float2 s1 = sm.get(cp, k1 == 0 ? ((L2 - k2) & (L2 - 1)) : (L2 - 1 - k2));
+    float2 x;
+    if (k == 0) {
+      x = make_float2(s0.x + s0.y, 0.f);
+      const long long aL = base + (long long)L2 * p.out.es;
+      p.out.re[aL] = s0.x - s0.y;
+      p.out.im[aL] = 0.f;
+    } else {
+      const float2 w = ldg2(p.rtw + k);
+      const float2 ha = make_float2(0.5f * (s0.x + s1.x), 0.5f * (s0.y - s1.y));
+      const float2 d = make_float2(0.5f * (s0.x - s1.x), 0.5f * (s0.y + s1.y));
+      x = cadd(ha, cmul_negi(cmul(d, w)));
+    }
+    const long long ad = base + (long long)k2 * p.out.es;
+    p.out.re[ad] = x.x;
+    p.out.im[ad] = x.y;
+  }
+}
+
 // The body of one CTA's work: lines [cta*C, cta*C + C) of the launch `p`.
 // UNIT: both element strides are 1 (split complex rows), so element offsets
 // are compile-time constants instead of runtime 64-bit products.
@@ -430,6 +509,11 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
   if constexpr (KIND == LK_R2C_HALF) {
     static_assert(COLS && !TSTORE && !TC, "the split R2C pass is a plain cols pass");
     r2c_half_body<LOGL, C>(p, cta);
+    return;
+  }
+  if constexpr (KIND == LK_R2C_PAIRED) {
+    static_assert(COLS && !TSTORE && !TC, "the paired R2C pass is a plain cols pass");
+    r2c_paired_body<LOGL, C>(p, cta);
     return;
   }
   using Sc = Sched<LOGL>;

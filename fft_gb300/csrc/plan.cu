@@ -536,9 +536,23 @@ std::unique_ptr<Plan> build_plan(int kind, int ndim, const long long* dims, long
         b.line(LK_C2R, false, false, logl, io(src, 1, 0, L + 1, 0, 0), io(realv, 1, 0, L, 0, 0), batch,
                false, 0, 0, 0, L);
     } else if (kind == K_R) {
-      // complex four-step into dst lines (stride L+1), then the real pass
-      b.axis(batch, L, 1, realv, dst, false, L, L + 1);
-      b.real_pass(io(dst, 1, 0, L + 1, 0, 0), io(dst, 1, 0, L + 1, 0, 0), batch, L, false, false);
+      // four-step pass A (twiddle, transposing store) into scratch, then
+      // pass B over mirrored column pairs with the real post-pass fused,
+      // into dst lines of L + 1 bins
+      const int logl = ilog2ll(L), l1 = AFFT_L1(logl), l2 = logl - l1;
+      const long long L1 = 1LL << l1, L2 = 1LL << l2;
+      View S = split_view(B_SCR, B_SCR, 0);
+      S.im.off = batch * L;
+      b.need_scratch(2 * batch * L);
+      b.line(LK_C2C, true, true, l1, io(realv, L2, 1, L, l2, L2 - 1), io(S, 1, L1, L, l2, L2 - 1), batch * L2,
+             false, L, L2 - 1, 0);
+      b.line(LK_R2C_PAIRED, true, false, l2, io(S, L1, 1, L, l1, L1 - 1), io(dst, L1, 1, L + 1, l1, L1 - 1),
+             batch * L1, false, 0, 0, 0, L);
+      if (b.ok) {
+        Op& ob = P->ops.back();
+        ob.p.pcols = L1;
+        if (L1 % ob.k.lines_per_cta) b.fail("paired pass: columns not a multiple of the tile");
+      }
     } else {
       // real pre-pass into scratch (Z'), then the inverse four-step from
       // there into dst's interleaved view, its own scratch above Z'
@@ -643,10 +657,10 @@ std::string describe_plan(const Plan& P) {
                "{\"type\":\"line\",\"logl\":%d,\"cols\":%d,\"lk\":%d,\"tstore\":%d,\"tc\":%d,\"C\":%d,"
                "\"halves\":%d,"
                "\"threads\":%d,\"smem\":%zu,\"grid\":%lld,\"nlines\":%lld,\"inverse\":%d,"
-               "\"tw_n\":%lld,\"tw_qmask\":%lld,\"tw_qshift\":%d,\"real_L\":%lld,",
+               "\"tw_n\":%lld,\"tw_qmask\":%lld,\"tw_qshift\":%d,\"real_L\":%lld,\"pcols\":%lld,",
                op.k.logl, op.k.cols, op.k.kind, op.k.tstore, op.k.tc, op.k.lines_per_cta, op.k.halves, op.threads,
                op.smem,
-               op.grid, op.p.nlines, op.p.inverse, op.p.tw_n, op.p.tw_qmask, op.p.tw_qshift, op.real_L);
+               op.grid, op.p.nlines, op.p.inverse, op.p.tw_n, op.p.tw_qmask, op.p.tw_qshift, op.real_L, op.p.pcols);
     } else if (op.type == OP_REAL) {
       snprintf(buf, sizeof buf,
                "{\"type\":\"real\",\"threads\":%d,\"grid\":%lld,\"nlines\":%lld,\"L\":%lld,"

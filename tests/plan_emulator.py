@@ -137,7 +137,28 @@ def run_op(B, op):
         halves = op.get("halves", 1)
         cta = q // op["C"] * halves
         lk = op["lk"]
-        if lk == 2:  # C2R: reads L+1 bins
+        if lk == 4:  # four-step pass B with the 1D real post-pass over mirrored column pairs
+            L1, C = op["pcols"], op["C"]
+            nt = op["nlines"] // L1
+            k1 = q % L1
+            H = C // 2
+            tile = np.where(k1 < L1 // 2, k1 // H, np.where(k1 == L1 // 2, 0, (L1 - k1) // H))
+            cta = (q // L1) * (L1 // C) + tile
+            x = _gather(B, acc, op["in"], q, np.arange(L), cta)
+            Xf = np.fft.fft(x, axis=1)
+            N = L1 * L
+            Z = Xf.reshape(nt, L1, L).transpose(0, 2, 1).reshape(nt, N)   # Z[o][k1 + L1 k2]
+            k = np.arange(N + 1)
+            s0 = Z[:, k % N]
+            s1 = Z[:, (N - k) % N]
+            X = (s0 + np.conj(s1)) / 2 - 0.5j * w(k, 2 * N) * (s0 - np.conj(s1))
+            X[:, 0] = Z[:, 0].real + Z[:, 0].imag
+            X[:, N] = Z[:, 0].real - Z[:, 0].imag
+            out = X[:, :N].reshape(nt, L, L1).transpose(0, 2, 1).reshape(nt * L1, L)
+            pending += _scatter(B, acc, op["out"], q, np.arange(L), cta, out)
+            q0 = np.arange(nt, dtype=np.int64) * L1
+            pending += _scatter(B, acc, op["out"], q0, np.array([L]), cta[q0], X[:, N:N + 1])
+        elif lk == 2:  # C2R: reads L+1 bins
             X = _gather(B, acc, op["in"], q, np.arange(L + 1), cta)
             i = np.arange(L)
             s0, s1 = X[:, i], X[:, L - i]
