@@ -29,6 +29,13 @@ bool get_cols_real(int logl, int kind, LineKernel* out) {
       case 10: *out = make_line_kernel<10, true, LK_R2C_PAIRED, false>(); return true;
       case 11: *out = make_line_kernel<11, true, LK_R2C_PAIRED, false>(); return true;
     }
+  } else if (kind == LK_C2R_PAIRED) {
+    // pass A of long 1D real inverses: L1 = 2^7 .. 2^9
+    switch (logl) {
+      case 7: *out = make_line_kernel<7, true, LK_C2R_PAIRED, true>(); return true;
+      case 8: *out = make_line_kernel<8, true, LK_C2R_PAIRED, true>(); return true;
+      case 9: *out = make_line_kernel<9, true, LK_C2R_PAIRED, true>(); return true;
+    }
   } else if (kind == LK_C2R) {
     switch (logl) {
       case 0: *out = make_line_kernel<0, true, LK_C2R, false>(); return true;

@@ -42,7 +42,9 @@ namespace agb {
 // LK_R2C_HALF: the cols R2C pass split over two CTAs per tile (below).
 // LK_R2C_PAIRED: pass B of a long 1D real forward with the real post-pass,
 // over tiles of mirrored column pairs (below).
-enum LineKind { LK_C2C = 0, LK_R2C = 1, LK_C2R = 2, LK_R2C_HALF = 3, LK_R2C_PAIRED = 4 };
+// LK_C2R_PAIRED: pass A of a long 1D real inverse with the real pre-pass,
+// over the same tiles (below).
+enum LineKind { LK_C2C = 0, LK_R2C = 1, LK_C2R = 2, LK_R2C_HALF = 3, LK_R2C_PAIRED = 4, LK_C2R_PAIRED = 5 };
 
 struct LineIO {
   float* re;
@@ -69,7 +71,7 @@ struct LineParams {
   int tw_qshift;
   int tw_lo_bits;
   const float2* rtw;        // real pass twiddles W_{2L}^k, k < L
-  long long pcols;          // LK_R2C_PAIRED: columns L1 of the four-step (lines per transform)
+  long long pcols;          // paired passes: lines per transform (L1 for pass B, L2 for pass A)
   int inverse;              // swap re/im on load and store
   const __half* tc_b;       // TC form: Mh then Ml, 32x32 FP16 each, [n][k]
   int* err;                 // TC form: error word set when a bounded wait gives up
@@ -425,6 +427,17 @@ __device__ __forceinline__ void r2c_half_body(const LineParams& p, long long cta
   }
 }
 
+// Column of slot c in a mirrored-pair tile (r2c_paired_body, c2r_paired_body): slots
+// 0 .. C/2-1 hold columns a + c, slots C/2 + m hold L1 - a - m, and in tile
+// 0 (a = 0) the slot C/2 holds L1/2.
+template <int C>
+__device__ __forceinline__ long long paired_column(int c, long long a, long long ncols) {
+  constexpr int H = C / 2;
+  if (c < H) return a + c;
+  const int m = c - H;
+  return (a == 0 && m == 0) ? ncols / 2 : ncols - a - m;
+}
+
 // Pass B of the four-step transform of a long 1D real forward (n/2 = L =
 // L1 L2 complex points of the interleaved view) with the real post-pass
 // (onedim.hpp:1058-1108) fused in.  Pass B line (o, k1) holds Z[k1 + L1 k2]
@@ -449,16 +462,8 @@ __device__ __forceinline__ void r2c_paired_body(const LineParams& p, long long c
   const long long L1 = p.pcols, tiles = L1 / C;
   const long long o = cta / tiles, a = (cta % tiles) * H;
   // this slot's column and its partner slot
-  long long k1;
-  int cp;
-  if (c < H) {
-    k1 = a + c;
-    cp = (a == 0 && c == 0) ? 0 : c + H;
-  } else {
-    const int m = c - H;
-    k1 = (a == 0 && m == 0) ? L1 / 2 : L1 - a - m;
-    cp = (a == 0 && m == 0) ? c : m;
-  }
+  const long long k1 = paired_column<C>(c, a, L1);
+  const int cp = c < H ? ((a == 0 && c == 0) ? 0 : c + H) : ((a == 0 && c == H) ? c : c - H);
   const long long q = o * L1 + k1;
 
   float2 v[E];
@@ -501,6 +506,77 @@ __device__ __forceinline__ void r2c_paired_body(const LineParams& p, long long c
   }
 }
 
+// Pass A of the inverse four-step of a long 1D real inverse (n/2 = L = L1 L2)
+// with the real pre-pass (onedim.hpp:1064-1068) fused into its loads.  Line
+// (o, t2) of pass A reads Z'[t2 + L2 t1], t1 < L1, and Z'[k] needs X[k] and
+// X[L - k]; for t2 > 0 the latter is element L1 - 1 - t1 of line
+// (o, L2 - t2), for t2 = 0 element (L1 - t1) of line (o, 0) (X[L] for
+// t1 = 0).  Tiles of mirrored column pairs (as in r2c_paired_body) keep both
+// reads inside one CTA, so the second hits the cache.  Then the ordinary pass
+// A work: inverse (re/im swapped) stages, the four-step twiddle and the
+// transposing store, all with the paired line mapping.
+template <int LOGL, int C>
+__device__ __forceinline__ void c2r_paired_body(const LineParams& p, long long cta) {
+  using Sc = Sched<LOGL>;
+  constexpr int L1 = Sc::L, E = Sc::E, T = Sc::T;
+  static_assert(C % 2 == 0 && T * C > 32, "paired tiles: even C, CTA-wide exchange");
+  extern __shared__ __align__(1024) float2 smem_raw[];
+  LineSmem<LOGL, C, true, true, false> sm{smem_raw};
+  const int tid = threadIdx.x;
+  const int c = tid % C, t = tid / C;
+  const long long L2 = p.pcols, tiles = L2 / C;
+  const long long o = cta / tiles, a = (cta % tiles) * (C / 2);
+  const long long t2 = paired_column<C>(c, a, L2);
+  const long long q = o * L2 + t2;
+
+  float2 v[E];
+  {
+    const long long base = line_off(p.in, q);
+    const long long pbase = line_off(p.in, o * L2 + ((L2 - t2) & (L2 - 1)));
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+      const int t1 = t + T * e;
+      const long long k = t2 + L2 * t1;
+      const long long a0 = base + (long long)t1 * p.in.es;
+      const long long a1 = t2 ? pbase + (long long)(L1 - 1 - t1) * p.in.es : base + (long long)(L1 - t1) * p.in.es;
+      const float2 s0 = make_float2(__ldg(p.in.re + a0), __ldg(p.in.im + a0));
+      const float2 s1 = make_float2(__ldg(p.in.re + a1), __ldg(p.in.im + a1));
+      float2 z;
+      if (k == 0) {
+        z = make_float2(s0.x + s1.x, s0.x - s1.x);
+      } else {
+        const float2 w = ldg2(p.rtw + k);
+        const float2 ha = cadd(s0, cconj(s1));
+        const float2 hb = cmul(csub(cconj(s1), s0), cconj(w));
+        z = cadd(ha, cmul_negi(hb));
+      }
+      v[e] = cswap(z);
+    }
+  }
+  run_stages<LOGL, C, true, false, 0>(v, t, c, p.tw, sm);
+
+  if constexpr (Sc::NSTAGES > 1) __syncthreads();
+#pragma unroll
+  for (int e = 0; e < E; e++) sm.put(c, t + T * e, v[e]);
+  __syncthreads();
+  const int c2 = tid / T, tt = tid % T;
+  const long long q2 = o * L2 + paired_column<C>(c2, a, L2);
+  const long long base = line_off(p.out, q2);
+  auto emit = [&](auto full) {
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+      const int k1 = tt + T * e;
+      float2 x = cmul(sm.get(c2, k1), fourstep_twiddle<L1, decltype(full)::value>(p, q2, k1));
+      x = cswap(x);
+      const long long ad = base + (long long)k1 * p.out.es;
+      p.out.re[ad] = x.x;
+      p.out.im[ad] = x.y;
+    }
+  };
+  if (p.tw_full) emit(std::true_type{});
+  else emit(std::false_type{});
+}
+
 // The body of one CTA's work: lines [cta*C, cta*C + C) of the launch `p`.
 // UNIT: both element strides are 1 (split complex rows), so element offsets
 // are compile-time constants instead of runtime 64-bit products.
@@ -514,6 +590,11 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
   if constexpr (KIND == LK_R2C_PAIRED) {
     static_assert(COLS && !TSTORE && !TC, "the paired R2C pass is a plain cols pass");
     r2c_paired_body<LOGL, C>(p, cta);
+    return;
+  }
+  if constexpr (KIND == LK_C2R_PAIRED) {
+    static_assert(COLS && TSTORE && !TC, "the paired C2R pass is pass A of a four-step");
+    c2r_paired_body<LOGL, C>(p, cta);
     return;
   }
   using Sc = Sched<LOGL>;

@@ -554,14 +554,39 @@ std::unique_ptr<Plan> build_plan(int kind, int ndim, const long long* dims, long
         if (L1 % ob.k.lines_per_cta) b.fail("paired pass: columns not a multiple of the tile");
       }
     } else {
-      // real pre-pass into scratch (Z'), then the inverse four-step from
-      // there into dst's interleaved view, its own scratch above Z'
-      View S = split_view(B_SCR, B_SCR, 0);
-      S.im.off = batch * L;
-      b.need_scratch(2 * batch * L);
-      b.real_pass(io(src, 1, 0, L + 1, 0, 0), io(S, 1, 0, L, 0, 0), batch, L, true, false);
-      b.scr_base = 2 * batch * L;
-      b.axis(batch, L, 1, S, realv, true, L, L);
+      const int logl = ilog2ll(L);
+      if (logl <= 19) {
+        // inverse four-step pass A over mirrored column pairs with the real
+        // pre-pass fused into its loads (twiddle, transposing store into
+        // scratch), then pass B into dst's interleaved view.  Pass A takes
+        // the shorter half, L1 <= 512: tiles of 16 lines, so each mirrored
+        // half-tile is a 32-byte row segment (8-line tiles of the longer
+        // lengths leave 16-byte halves, measured slower than the unfused
+        // form below)
+        const int l1 = logl / 2, l2 = logl - l1;
+        const long long L1 = 1LL << l1, L2 = 1LL << l2;
+        View S = split_view(B_SCR, B_SCR, 0);
+        S.im.off = batch * L;
+        b.need_scratch(2 * batch * L);
+        b.line(LK_C2R_PAIRED, true, true, l1, io(src, L2, 1, L + 1, l2, L2 - 1), io(S, 1, L1, L, l2, L2 - 1),
+               batch * L2, true, L, L2 - 1, 0, L);
+        if (b.ok) {
+          Op& oa = P->ops.back();
+          oa.p.pcols = L2;
+          if (L2 % oa.k.lines_per_cta) b.fail("paired pass: columns not a multiple of the tile");
+        }
+        b.line(LK_C2C, true, false, l2, io(S, L1, 1, L, l1, L1 - 1), io(realv, L1, 1, L, l1, L1 - 1),
+               batch * L1, true);
+      } else {
+        // real pre-pass into scratch (Z'), then the inverse four-step from
+        // there into dst's interleaved view, its own scratch above Z'
+        View S = split_view(B_SCR, B_SCR, 0);
+        S.im.off = batch * L;
+        b.need_scratch(2 * batch * L);
+        b.real_pass(io(src, 1, 0, L + 1, 0, 0), io(S, 1, 0, L, 0, 0), batch, L, true, false);
+        b.scr_base = 2 * batch * L;
+        b.axis(batch, L, 1, S, realv, true, L, L);
+      }
     }
   } else {
     // N-D real, dim 0 halved
@@ -757,7 +782,7 @@ bool get_line_kernel(int logl, bool cols, int kind, bool tstore, LineKernel* out
   }
   if (logl > COLS_MAX_LOG) return false;
   if (kind == LK_C2C) return get_cols_c2c(logl, tstore, out);
-  if (tstore) return false;
+  if (tstore != (kind == LK_C2R_PAIRED)) return false;
   return get_cols_real(logl, kind, out);
 }
 

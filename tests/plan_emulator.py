@@ -158,6 +158,27 @@ def run_op(B, op):
             pending += _scatter(B, acc, op["out"], q, np.arange(L), cta, out)
             q0 = np.arange(nt, dtype=np.int64) * L1
             pending += _scatter(B, acc, op["out"], q0, np.array([L]), cta[q0], X[:, N:N + 1])
+        elif lk == 5:  # inverse four-step pass A with the 1D real pre-pass over mirrored column pairs
+            L2c, C = op["pcols"], op["C"]
+            nt = op["nlines"] // L2c
+            t2 = q % L2c
+            H = C // 2
+            tile = np.where(t2 < L2c // 2, t2 // H, np.where(t2 == L2c // 2, 0, (L2c - t2) // H))
+            cta = (q // L2c) * (L2c // C) + tile
+            N = L2c * L
+            x = _gather(B, acc, op["in"], q, np.arange(L), cta)            # X[t2 + L2 t1]
+            xl = _gather(B, acc, op["in"], np.arange(nt, dtype=np.int64) * L2c, np.array([L]),
+                         cta[np.arange(nt) * L2c])                          # X[N]
+            X = np.concatenate([x.reshape(nt, L2c, L).transpose(0, 2, 1).reshape(nt, N), xl], axis=1)
+            k = np.arange(N)
+            s0, s1 = X[:, k], X[:, N - k]
+            Zp = (s0 + np.conj(s1)) - 1j * (np.conj(s1) - s0) * np.conj(w(k, 2 * N))
+            Zp[:, 0] = (X[:, 0].real + X[:, N].real) + 1j * (X[:, 0].real - X[:, N].real)
+            z = Zp.reshape(nt, L, L2c).transpose(0, 2, 1).reshape(nt * L2c, L)   # line (o, t2), element t1
+            Xf = np.fft.ifft(z, axis=1) * L
+            tw = w(t2[:, None] * np.arange(L)[None, :], op["tw_n"])
+            Xf = Xf * np.conj(tw)
+            pending += _scatter(B, acc, op["out"], q, np.arange(L), cta, Xf)
         elif lk == 2:  # C2R: reads L+1 bins
             X = _gather(B, acc, op["in"], q, np.arange(L + 1), cta)
             i = np.arange(L)

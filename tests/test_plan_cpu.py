@@ -60,7 +60,8 @@ def test_launch_counts():
     assert len(describe("c", [1 << 16], 4)["ops"]) == 2
     assert len(describe("c", [256, 256, 256])["ops"]) == 3
     assert len(describe("r", [4096, 4096])["ops"]) == 2
-    # long 1D real: the real post-pass rides in pass B; the inverse keeps a
-    # standalone pre-pass
+    # long 1D real: the real post-pass rides in pass B, the pre-pass of the
+    # inverse in pass A
     assert len(describe("r", [1 << 20], 2)["ops"]) == 2
-    assert len(describe("ri", [1 << 20], 2)["ops"]) == 3
+    assert len(describe("ri", [1 << 20], 2)["ops"]) == 2
+    assert len(describe("ri", [1 << 22], 1)["ops"]) == 3
