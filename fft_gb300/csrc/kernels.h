@@ -6,7 +6,7 @@
 namespace agb {
 
 typedef void (*LineKernelFn)(LineParams);
-typedef void (*GroupedKernelFn)(const Segment*, int, long long);
+typedef void (*GroupedKernelFn)(const Segment*, const int*, long long);
 
 struct LineKernel {
   LineKernelFn fn;

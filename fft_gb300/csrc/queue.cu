@@ -5,10 +5,11 @@
 // resolved against the transform's own pointers into concrete launch
 // segments: pass i of a transform becomes a segment of "level" i.  Segments
 // are grouped by (level, kernel shape) into device-side descriptor tables;
-// each group is ONE persistent launch (line_fft_grouped or
-// elementwise_grouped) whose CTAs walk the table.  Groups of one level are
-// independent and become parallel branches of a CUDA graph; levels follow
-// each other.  The first run captures the graph, later runs replay it.
+// each group is ONE launch (line_fft_grouped or elementwise_grouped) of one
+// CTA per virtual CTA, which finds its segment in a per-virtual-CTA map.
+// Groups of one level are independent and become parallel branches of a
+// CUDA graph; levels follow each other.  The first run captures the graph,
+// later runs replay it.
 //
 // Scratch for transforms whose plans need it (four-step passes, real
 // inverse of N-D arrays) comes from one queue-owned arena, a disjoint region
@@ -33,6 +34,7 @@ struct Group {
   std::vector<EwSegment> esegs;
   long long total = 0;   // virtual CTAs / blocks
   void* d_tab = nullptr;
+  int* d_map = nullptr;  // segment of each virtual CTA / block
   int grid = 0, threads = 0;
   size_t smem = 0;
 };
@@ -50,8 +52,10 @@ struct QueueImpl {
   int device = 0;
   ~QueueImpl() {
     if (exec) cudaGraphExecDestroy(exec);
-    for (auto& g : groups)
+    for (auto& g : groups) {
       if (g.d_tab) cudaFree(g.d_tab);
+      if (g.d_map) cudaFree(g.d_map);
+    }
     if (arena) cudaFree(arena);
     for (auto s : pool) cudaStreamDestroy(s);
     for (auto e : events) cudaEventDestroy(e);
@@ -72,8 +76,6 @@ static LineIO bind_io(const IOSpec& s, float* const* base) {
 }
 
 static int build_queue(QueueImpl& Q) {
-  int nsm = 0;
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, Q.device);
   // plans and scratch layout
   std::vector<std::shared_ptr<Plan>> plan_of;
   std::vector<long long> scr_off;
@@ -172,9 +174,7 @@ static int build_queue(QueueImpl& Q) {
         set_error(AFFT_GB300_ECUDA, "kernel shared memory configuration failed");
         return AFFT_GB300_ECUDA;
       }
-      int per_sm = 1;
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, g.k.grouped, g.threads, g.smem);
-      g.grid = (int)std::min<long long>(g.total, (long long)std::max(per_sm, 1) * nsm);
+      g.grid = (int)g.total;
     } else {
       std::stable_sort(g.esegs.begin(), g.esegs.end(),
                        [](const EwSegment& a, const EwSegment& b) { return a.blk0 > b.blk0; });
@@ -188,10 +188,25 @@ static int build_queue(QueueImpl& Q) {
       host = g.esegs.data();
       bytes = g.esegs.size() * sizeof(EwSegment);
       g.threads = 256;
-      g.grid = (int)std::min<long long>(g.total, 8LL * nsm);
+      g.grid = (int)g.total;
+    }
+    if (g.total > 0x7fffffffLL) {
+      set_error(AFFT_GB300_EINVAL, "queue group too large for one launch");
+      return AFFT_GB300_EINVAL;
+    }
+    // the segment of every virtual CTA / block (segments are in cta0 order)
+    std::vector<int> map((size_t)g.total);
+    const size_t nseg = g.line ? g.segs.size() : g.esegs.size();
+    for (size_t i = 0; i < nseg; i++) {
+      const long long b0 = g.line ? g.segs[i].cta0 : g.esegs[i].blk0;
+      const long long b1 = i + 1 < nseg ? (g.line ? g.segs[i + 1].cta0 : g.esegs[i + 1].blk0) : g.total;
+      std::fill(map.begin() + b0, map.begin() + b1, (int)i);
     }
     if (cudaMalloc(&g.d_tab, bytes) != cudaSuccess ||
-        cudaMemcpy(g.d_tab, host, bytes, cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaMemcpy(g.d_tab, host, bytes, cudaMemcpyHostToDevice) != cudaSuccess ||
+        (g.total && (cudaMalloc(&g.d_map, map.size() * sizeof(int)) != cudaSuccess ||
+                     cudaMemcpy(g.d_map, map.data(), map.size() * sizeof(int), cudaMemcpyHostToDevice) !=
+                         cudaSuccess))) {
       cudaGetLastError();
       set_error(AFFT_GB300_ENOMEM, "queue descriptor upload failed");
       return AFFT_GB300_ENOMEM;
@@ -206,9 +221,9 @@ static int build_queue(QueueImpl& Q) {
 static void launch_group(const Group& g, cudaStream_t st) {
   if (g.total == 0) return;
   if (g.line)
-    g.k.grouped<<<g.grid, g.threads, g.smem, st>>>((const Segment*)g.d_tab, (int)g.segs.size(), g.total);
+    g.k.grouped<<<g.grid, g.threads, g.smem, st>>>((const Segment*)g.d_tab, g.d_map, g.total);
   else
-    elementwise_grouped<<<g.grid, g.threads, 0, st>>>((const EwSegment*)g.d_tab, (int)g.esegs.size(), g.total);
+    elementwise_grouped<<<g.grid, g.threads, 0, st>>>((const EwSegment*)g.d_tab, g.d_map, g.total);
 }
 
 static int capture(QueueImpl& Q) {

@@ -108,15 +108,10 @@ __global__ void real1_kernel(const RealPassParams p) {
   real1_body(p, (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
-__global__ void elementwise_grouped(const EwSegment* __restrict__ segs, int nseg, long long total) {
+__global__ void elementwise_grouped(const EwSegment* __restrict__ segs, const int* __restrict__ seg_of,
+                                    long long total) {
   for (long long v = blockIdx.x; v < total; v += gridDim.x) {
-    int lo = 0, hi = nseg - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (segs[mid].blk0 <= v) lo = mid;
-      else hi = mid - 1;
-    }
-    const EwSegment& s = segs[lo];
+    const EwSegment& s = segs[__ldg(seg_of + v)];
     const long long idx = (v - s.blk0) * blockDim.x + threadIdx.x;
     if (s.type == EW_REAL) real_pass_body(s.rp, idx);
     else if (s.type == EW_COPY) copy_body(s.cp, idx);
