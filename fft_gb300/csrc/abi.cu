@@ -195,6 +195,49 @@ static bool is_device_ptr(const void* p) {
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+// Pinned host memory that kernels can reach at the same address (page-locked
+// and mapped: cudaHostAlloc / cudaHostRegister, unified addressing).
+static bool is_mapped_host_ptr(const void* p) {
+  if (!p) return true;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost && a.devicePointer == p;
+}
+
+// Whether a launch's accesses to a caller array suit the host link: whole
+// lines (rows mode) or tiles of at least 16 adjacent lines (64-byte or wider
+// row segments).  Narrower segments crawl across the link (a 64 x 2^20 real
+// transform, whose passes touch host memory in 32-byte pieces, ran 3.5x
+// slower end to end than with staged copies).
+static bool host_access_ok(const Op& op) {
+  if (op.type != OP_LINE) return false;
+  if (!op.k.cols) return true;
+  return op.k.kind == LK_C2C && op.k.lines_per_cta >= 16;
+}
+
+// A plan can run on mapped host buffers directly when the caller's arrays are
+// touched once each: only the first launch reads src, only the last writes
+// dst, and nothing reads dst (no in-place passes over it).  Each element then
+// crosses the host link once in each direction, as with staged copies, but
+// without the staging buffers and with transfer and compute overlapped.
+static bool host_direct_ok(const Plan& P) {
+  const size_t n = P.ops.size();
+  if (n == 0 || !host_access_ok(P.ops[0]) || !host_access_ok(P.ops[n - 1])) return false;
+  for (size_t i = 0; i < n; i++) {
+    const Op& op = P.ops[i];
+    auto is_src = [](int b) { return b == B_SRC_RE || b == B_SRC_IM; };
+    auto is_dst = [](int b) { return b == B_DST_RE || b == B_DST_IM; };
+    if ((is_src(op.in.re.buf) || is_src(op.in.im.buf)) && i != 0) return false;
+    if (is_dst(op.in.re.buf) || is_dst(op.in.im.buf)) return false;
+    if ((is_dst(op.out.re.buf) || is_dst(op.out.im.buf)) && i != n - 1) return false;
+    if (is_src(op.out.re.buf) || is_src(op.out.im.buf)) return false;
+  }
+  return n > 0;
+}
+
 // Elements per array of one call: input and output, for each data argument
 static void io_elems(const Plan& P, long long* in_n, long long* out_n) {
   *in_n = P.in_elems * P.batch;
@@ -236,6 +279,20 @@ static int transform_sync(void* plan, const float* sr, const float* si, float* d
       return AFFT_GB300_ECUDA;
     }
     return check_tc_error(*P);
+  }
+  // pinned host data the kernels can reach: run on it directly when the
+  // plan touches each caller array once
+  bool mapped = is_mapped_host_ptr(sr) && is_mapped_host_ptr(dr) && (!use_si || is_mapped_host_ptr(si)) &&
+                (!use_di || is_mapped_host_ptr(di));
+  if (mapped && P->form != FORM_TC && host_direct_ok(*P)) {
+    int rc = P->launch(sr, use_si ? si : nullptr, dr, use_di ? di : nullptr, P->stream);
+    if (rc) return rc;
+    cudaError_t e = cudaStreamSynchronize(P->stream);
+    if (e != cudaSuccess) {
+      set_error(AFFT_GB300_ECUDA, cudaGetErrorString(e));
+      return AFFT_GB300_ECUDA;
+    }
+    return 0;
   }
   // host data: stage through plan-owned device buffers.  A batch is cut
   // into chunks so the copy of chunk i+1 in, the transform of chunk i and the

@@ -152,6 +152,52 @@ def test_golden_host_pointers(golden, dev):
         check(kind, dims, a, b, run_plan(kind, dims, a, b, dev, host=True))
 
 
+@pytest.mark.parametrize("kind,dims", [("c", [4096]), ("ci", [1 << 16]), ("r", [1 << 20]), ("ri", [1 << 16]),
+                                       ("r", [2048]), ("c", [256, 256]), ("ri", [64, 64, 64])], ids=str)
+@pytest.mark.parametrize("fmt", [G.afft_split, G.afft_interleaved], ids=["split", "inter"])
+def test_pinned_host_buffers(kind, dims, fmt, dev):
+    # pinned host arrays: the kernels read and write them directly when the
+    # plan touches each array once, else they are staged; both must match
+    a, b = inputs(kind, dims, 23)
+    plan = {"c": G.complex_transform, "ci": G.inverse_complex_transform,
+            "r": G.real_transform, "ri": G.inverse_real_transform}[kind](dims, fmt=fmt)
+    n = int(np.prod(dims))
+    h = O.half_elems(dims)
+    inter = fmt == G.afft_interleaved
+    pin = lambda x: torch.from_numpy(np.ascontiguousarray(x, np.float32)).pin_memory()
+    zeros = lambda m: torch.zeros(m, dtype=torch.float32).pin_memory()
+    if kind in ("c", "ci"):
+        if inter:
+            src = np.empty(2 * n, np.float32)
+            src[0::2], src[1::2] = a, b
+            d = zeros(2 * n)
+            plan(pin(src), None, d, None)
+            got = (d.numpy()[0::2].copy(), d.numpy()[1::2].copy())
+        else:
+            dr, di = zeros(n), zeros(n)
+            plan(pin(a), pin(b), dr, di)
+            got = (dr.numpy(), di.numpy())
+    elif kind == "r":
+        if inter:
+            d = zeros(2 * h)
+            plan(pin(a), d, None)
+            got = (d.numpy()[0::2].copy(), d.numpy()[1::2].copy())
+        else:
+            dr, di = zeros(h), zeros(h)
+            plan(pin(a), dr, di)
+            got = (dr.numpy(), di.numpy())
+    else:
+        d = zeros(n)
+        if inter:
+            src = np.empty(2 * h, np.float32)
+            src[0::2], src[1::2] = a, b
+            plan(pin(src), None, d)
+        else:
+            plan(pin(a), pin(b), d)
+        got = d.numpy()
+    check(kind, dims, a, b, got)
+
+
 # --- shapes beyond the fixtures ---------------------------------------------
 
 ONE_D = [2 ** k for k in range(0, 21)]
