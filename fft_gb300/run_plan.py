@@ -1,0 +1,43 @@
+"""Run one batched plan on seeded device data a few times, for profiling.
+
+    python -m fft_gb300.run_plan KIND DIMS BATCH [REPS]
+
+KIND is c, ci, r or ri; DIMS a JSON list such as [256,256,256].  Each
+repetition launches the plan's kernels once on the CUDA default stream;
+the script synchronises at the end and prints the launches per transform.
+"""
+import json
+import sys
+
+import torch
+
+from . import BatchPlan
+
+
+def main(argv):
+    if len(argv) < 3:
+        print(__doc__)
+        return 2
+    kind, dims, batch = argv[0], json.loads(argv[1]), int(argv[2])
+    reps = int(argv[3]) if len(argv) > 3 else 2
+    n = 1
+    for d in dims:
+        n *= d
+    h = (dims[0] // 2 + 1) * (n // dims[0])
+    plan = BatchPlan(kind, dims, batch)
+    g = torch.Generator(device="cuda").manual_seed(n + batch)
+    nin = (h if kind == "ri" else n) * batch
+    nout = (h if kind == "r" else n) * batch
+    a = torch.randn(nin, device="cuda", generator=g)
+    b = torch.randn(nin, device="cuda", generator=g)
+    oa = torch.empty(nout, device="cuda")
+    ob = torch.empty_like(oa)
+    for _ in range(reps):
+        plan.launch(a, None if kind == "r" else b, oa, None if kind == "ri" else ob)
+    torch.cuda.synchronize()
+    print("launches per transform", plan.launches)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main(sys.argv[1:]))
