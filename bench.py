@@ -12,9 +12,14 @@ value      GFLOP/s by afft's convention (5 N log2 N complex, 2.5 N log2 N
            real, testing.cpp:1027), inputs resident in HBM, CUDA events on
            the launching stream, max over ranks.
 e2e        the same metric through the C ABI with pinned HOST buffers: each
-           call stages its input to the device and its result back.
-roofline   the dominant kernel's algorithmic bytes per launch / its mean
-           launch time (CUDA events), against the measured HBM copy peak.
+           call moves its input to the device and its result back (staged
+           copies, or the kernels' own accesses over the host link when the
+           plan touches each array once in wide segments).
+roofline   the forward plan's algorithmic bytes (one read + one write of the
+           data) / its time (CUDA events), against the measured HBM copy
+           peak; "passes" divides the same time into what the plan's launches
+           must move between them (each reads its input and writes its output
+           once), i.e. how close multi-pass plans run to the peak per pass.
 cpu_baseline  the oracle's FP32 port of afft on the host cores (bounded
            sample of the same workload).
 --impl reference  times that CPU port alone (all host threads), same metric.
@@ -384,6 +389,11 @@ def run_ours(args, cfg):
     hbm, peak_src = peaks()
     alg_bytes = bytes_of(kind, dims, batch)
     achieved = alg_bytes / (fwd_ms / 1e3) / 1e9
+    # the same time against what the plan's passes must move between them
+    # (each launch reads its input and writes its output once)
+    pb = G.pass_bytes(G.describe(kind, dims, batch))
+    passes = {"launches": fwd.launches, "bytes": pb, "achieved": round(pb / (fwd_ms / 1e3) / 1e9, 1),
+              "frac": round(pb / (fwd_ms / 1e3) / 1e9 / hbm, 4), "unit": "GB/s"}
     cpu = None
     if not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -403,7 +413,8 @@ def run_ours(args, cfg):
                      "traffic": args.traffic if args.traffic else (measured_traffic(cfg) if not args.batch and args.form == "plain" else None),
                      "peak_source": peak_src,
                      "kernel": "forward plan (%d launch%s), %.4f ms per launch" % (
-                         fwd.launches, "es" if fwd.launches > 1 else "", fwd_ms / fwd.launches)},
+                         fwd.launches, "es" if fwd.launches > 1 else "", fwd_ms / fwd.launches),
+                     "passes": passes},
         "cpu_baseline": cpu,
         "e2e": e2e,
         "tc_split_form": tc_form,

@@ -132,6 +132,44 @@ def ptr(a):
     raise TypeError(type(a))
 
 
+def describe(kind, dims, batch=1, fmt=0):
+    """The kernel launches a batched plan issues, as a dict (from
+    afft_gb300_plan_describe; no device needed)."""
+    import json
+    L = lib()
+    k = KINDS[kind] if isinstance(kind, str) else kind
+    arr, n = _dims(dims)
+    size = L.afft_gb300_plan_describe(k, n, arr, batch, fmt, None, 0)
+    if size == 0:
+        _check("plan_describe")
+        raise AfftError("plan_describe rejected the plan")
+    buf = ctypes.create_string_buffer(size)
+    L.afft_gb300_plan_describe(k, n, arr, batch, fmt, buf, size)
+    return json.loads(buf.value.decode())
+
+
+def pass_bytes(desc):
+    """Bytes the launches of a described plan must move between them: one
+    read of each launch's input and one write of its output (split FP32,
+    8 bytes per complex element), summed over launches."""
+    total = 0
+    for op in desc["ops"]:
+        t = op["type"]
+        if t == "line":
+            L, n, lk = 1 << op["logl"], op["nlines"], op["lk"]
+            if lk in (1, 2):          # real forward / inverse: L complex one way, L + 1 the other
+                total += n * 8 * (2 * L + 1)
+            else:                     # complex, and the paired real passes of long 1D axes
+                total += n * 16 * L
+        elif t == "real":
+            total += op["nlines"] * 8 * (2 * op["L"] + 1)
+        elif t == "copy":
+            total += op["nlines"] * 16 * op["len"]
+        else:                         # length-1 real transforms
+            total += op["nlines"] * 12
+    return total
+
+
 def _dims(dims):
     dims = [int(d) for d in dims]
     return (ctypes.c_size_t * max(1, len(dims)))(*dims), len(dims)
