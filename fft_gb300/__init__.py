@@ -84,6 +84,10 @@ def lib():
         L.afft_gb300_queue_create_ex.argtypes = [P, S, I]
         L.afft_gb300_plan_describe.restype = S
         L.afft_gb300_plan_describe.argtypes = [I, S, P, S, I, ctypes.c_char_p, S]
+        L.afft_gb300_tune.restype = I
+        L.afft_gb300_tune.argtypes = [I, S, P, S, I, ctypes.c_char_p, S]
+        L.afft_gb300_tuned.restype = I
+        L.afft_gb300_tuned.argtypes = [I, S, P, S, I, P, P]
         L.afft_gb300_c2c_noalloc.restype = I
         L.afft_gb300_c2c_noalloc.argtypes = [P, P, P, P, S, S, I, P]
         L.afft_gb300_queue_run.restype = I
@@ -146,6 +150,33 @@ def describe(kind, dims, batch=1, fmt=0):
     buf = ctypes.create_string_buffer(size)
     L.afft_gb300_plan_describe(k, n, arr, batch, fmt, buf, size)
     return json.loads(buf.value.decode())
+
+
+def tune(kind, dims, batch=1, fmt=afft_split):
+    """Run the autotuner for a shape on the current device (afft_gb300_tune);
+    returns its report: the candidates with median times and the choice."""
+    import json
+    L = lib()
+    k = KINDS[kind] if isinstance(kind, str) else kind
+    arr, n = _dims(dims)
+    buf = ctypes.create_string_buffer(8192)
+    if L.afft_gb300_tune(k, n, arr, batch, fmt, buf, len(buf)):
+        _check("tune")
+        raise AfftError("tune failed")
+    return json.loads(buf.value.decode())
+
+
+def tuned(kind, dims, batch=1, fmt=afft_split):
+    """The autotuner's choice for a shape, {"split", "real_inv"}, or None."""
+    L = lib()
+    k = KINDS[kind] if isinstance(kind, str) else kind
+    arr, n = _dims(dims)
+    a, b = ctypes.c_int(), ctypes.c_int()
+    r = L.afft_gb300_tuned(k, n, arr, batch, fmt, ctypes.byref(a), ctypes.byref(b))
+    if r < 0:
+        _check("tuned")
+        raise AfftError("bad shape")
+    return {"split": a.value, "real_inv": b.value} if r == 1 else None
 
 
 def pass_bytes(desc):

@@ -291,7 +291,13 @@ struct Builder {
   std::string err;
   long long scr_base = 0;  // floats of scratch reserved below four-step use
   bool dry = false;        // describe only: no device tables
+  Tuning tune;             // plan variant
   explicit Builder(Plan& p, bool d = false) : P(p), dry(d) {}
+
+  // four-step split of an axis of 2^logl points: L1 takes the larger half
+  // (measured the better default on GB300 for odd logl), or the smaller one
+  // when tuned so
+  int l1_of(int logl) const { return tune.split ? logl / 2 : AFFT_L1(logl); }
 
   void fail(const std::string& m) {
     if (ok) err = m;
@@ -426,7 +432,7 @@ struct Builder {
         return;
       }
       // four-step along a contiguous axis
-      int l1 = AFFT_L1(logl), l2 = logl - l1;
+      int l1 = l1_of(logl), l2 = logl - l1;
       if (l1 > COLS_MAX_LOG || l2 > COLS_MAX_LOG) {
         fail("axis longer than 2^22 points");
         return;
@@ -450,7 +456,7 @@ struct Builder {
       return;
     }
     // four-step along a strided axis
-    int l1 = AFFT_L1(logl), l2 = logl - l1;
+    int l1 = l1_of(logl), l2 = logl - l1;
     if (l1 > COLS_MAX_LOG || l2 > COLS_MAX_LOG) {
       fail("axis longer than 2^22 points");
       return;
@@ -492,7 +498,7 @@ struct Builder {
 };
 
 std::unique_ptr<Plan> build_plan(int kind, int ndim, const long long* dims, long long batch, int format,
-                                 bool dry, int form) {
+                                 bool dry, int form, const Tuning* tune) {
   std::unique_ptr<Plan> P(new Plan());
   P->kind = kind;
   P->format = format;
@@ -513,6 +519,8 @@ std::unique_ptr<Plan> build_plan(int kind, int ndim, const long long* dims, long
   View dst = inter ? inter_view(B_DST_RE) : split_view(B_DST_RE, B_DST_IM);
 
   Builder b(*P, dry);
+  if (tune) b.tune = *tune;
+  else if (!dry && form == 0) b.tune = tuned_choice(kind, ndim, dims, batch, format);
   if (kind == K_C || kind == K_CI) {
     P->in_elems = N;
     P->out_elems = N;
@@ -539,7 +547,7 @@ std::unique_ptr<Plan> build_plan(int kind, int ndim, const long long* dims, long
       // four-step pass A (twiddle, transposing store) into scratch, then
       // pass B over mirrored column pairs with the real post-pass fused,
       // into dst lines of L + 1 bins
-      const int logl = ilog2ll(L), l1 = AFFT_L1(logl), l2 = logl - l1;
+      const int logl = ilog2ll(L), l1 = b.l1_of(logl), l2 = logl - l1;
       const long long L1 = 1LL << l1, L2 = 1LL << l2;
       View S = split_view(B_SCR, B_SCR, 0);
       S.im.off = batch * L;
@@ -555,7 +563,10 @@ std::unique_ptr<Plan> build_plan(int kind, int ndim, const long long* dims, long
       }
     } else {
       const int logl = ilog2ll(L);
-      if (logl <= 19) {
+      // the paired pass A runs over the shorter half by default (the longer
+      // one when tuned so, where its kernel exists: pass A lengths <= 512)
+      const int l1p = b.tune.split ? (logl + 1) / 2 : logl / 2;
+      if (logl <= 19 && b.tune.real_inv == 0 && l1p <= 9) {
         // inverse four-step pass A over mirrored column pairs with the real
         // pre-pass fused into its loads (twiddle, transposing store into
         // scratch), then pass B into dst's interleaved view.  Pass A takes
@@ -563,7 +574,7 @@ std::unique_ptr<Plan> build_plan(int kind, int ndim, const long long* dims, long
         // half-tile is a 32-byte row segment (8-line tiles of the longer
         // lengths leave 16-byte halves, measured slower than the unfused
         // form below)
-        const int l1 = logl / 2, l2 = logl - l1;
+        const int l1 = l1p, l2 = logl - l1;
         const long long L1 = 1LL << l1, L2 = 1LL << l2;
         View S = split_view(B_SCR, B_SCR, 0);
         S.im.off = batch * L;

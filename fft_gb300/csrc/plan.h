@@ -87,11 +87,25 @@ struct Plan {
              cudaStream_t stream);
 };
 
+// Plan variants the autotuner chooses between (tune.cu).  split: 0 the
+// built-in four-step split of long axes, 1 the other half first; real_inv:
+// 0 the fused paired pre-pass for long 1D real inverses where it applies,
+// 1 the standalone pre-pass.
+struct Tuning {
+  int split = 0;
+  int real_inv = 0;
+};
+// The tuned choice for a shape on the current device, if the autotuner has
+// one (tuning it first when AFFT_GB300_AUTOTUNE=1); else the defaults.
+Tuning tuned_choice(int kind, int ndim, const long long* dims, long long batch, int format);
+
 // Build a plan; returns nullptr and sets the error on failure.
 // dry: build the op list only (no device calls, twiddle pointers null), for
 // describing a plan without a GPU.
+// tune: the variant to build; nullptr = the tuned choice for device plans of
+// the plain form, the defaults otherwise.
 std::unique_ptr<Plan> build_plan(int kind, int ndim, const long long* dims, long long batch,
-                                 int format, bool dry = false, int form = 0);
+                                 int format, bool dry = false, int form = 0, const Tuning* tune = nullptr);
 // TC form: the DFT-16 matrix tiles (Mh, Ml) and the per-device error word
 const __half* tc_matrix_table();
 int* tc_error_word();

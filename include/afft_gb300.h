@@ -215,6 +215,26 @@ AFFT_GB300_API int afft_gb300_release(void* plan);
 AFFT_GB300_API size_t afft_gb300_plan_describe(int kind, size_t ndim,
   const size_t* dim, size_t batch, int format, char* buf, size_t buflen);
 
+/* Autotuner (no counterpart in afft): times the plan variants a shape allows
+ * on the current device and keeps the fastest for later plans of the same
+ * (device, kind, dims, batch, format).  The variants are the four-step split
+ * of axes longer than one CTA holds (which half the first pass takes) and,
+ * for long 1D real inverses, the real pre-pass fused into the first pass or
+ * run on its own.  It allocates scratch device buffers for the timing.
+ * Choices are kept for the process and, when the environment variable
+ * AFFT_GB300_TUNE_CACHE names a file, stored there and reloaded on first use;
+ * with AFFT_GB300_AUTOTUNE=1 every new shape is tuned when its first plan is
+ * built.  Plans built before a choice exists use the built-in defaults, and
+ * afft_gb300_plan_describe always describes the defaults.  `report` (may be
+ * NULL) receives a JSON summary: the candidates with their median times and
+ * the choice.  Returns 0 or an AFFT_GB300_* code. */
+AFFT_GB300_API int afft_gb300_tune(int kind, size_t ndim, const size_t* dim, size_t batch, int format,
+  char* report, size_t report_len);
+/* The autotuner's choice for a shape on the current device: 1 and the
+ * variant (split, real_inv) if one is known, 0 if not, -1 for a bad shape. */
+AFFT_GB300_API int afft_gb300_tuned(int kind, size_t ndim, const size_t* dim, size_t batch, int format,
+  int* split, int* real_inv);
+
 /* Self-test of the library's bounded device waits (no counterpart in afft):
  * launches a kernel that waits on a barrier nothing releases, for `iters`
  * polls, and returns AFFT_GB300_ETIMEOUT when the kernel gave up and
