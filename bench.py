@@ -163,6 +163,36 @@ def rank_seed(rank):
     return 1234 + rank
 
 
+def accuracy(kind, dims, batch, src, mid, back, with_inv):
+    """Relative L2 and max error (max |y - ref| / max |ref|) of the forward
+    outputs of a sample of the batch against numpy's float64 FFT, and of the
+    unnormalised round trip inverse(forward(x)) / n against x."""
+    n = int(np.prod(dims))
+    d = [x for x in dims if x != 1] or [1]
+    h = (d[0] // 2 + 1) * (n // d[0])
+    k = max(1, min(batch, (1 << 22) // max(n, 1)))   # transforms in the sample
+    x = src[0][:k * n].double().cpu().numpy()
+    if kind == "c":
+        x = x + 1j * src[1][:k * n].double().cpu().numpy()
+    shape = [k] + list(d)
+    ref = np.fft.fftn(x.reshape(shape), axes=list(range(1, len(shape))))
+    if kind != "c":
+        ref = ref[:, :d[0] // 2 + 1]
+    m = h if kind != "c" else n
+    y = mid[0][:k * m].double().cpu().numpy() + 1j * mid[1][:k * m].double().cpu().numpy()
+    ref = ref.reshape(-1)
+    out = {"sample": "%d of %d transforms" % (k, batch), "reference": "numpy float64 FFT",
+           "rel_l2": float(np.linalg.norm(y - ref) / np.linalg.norm(ref)),
+           "max_err": float(np.abs(y - ref).max() / np.abs(ref).max())}
+    if with_inv:
+        xb = back[0][:k * n].double().cpu().numpy()
+        if kind == "c":
+            xb = xb + 1j * back[1][:k * n].double().cpu().numpy()
+        xb = xb / n
+        out["round_trip_rel_l2"] = float(np.linalg.norm(xb - x) / np.linalg.norm(x))
+    return out
+
+
 def make_inputs(kind, dims, batch, seed, dev):
     import torch
     n = int(np.prod(dims))
@@ -370,6 +400,9 @@ def run_ours(args, cfg):
     per_step_flops = flops_of(kind, dims, batch) * (2 if inv else 1)
     value = per_step_flops * world / (ms_step / 1e3) / 1e9
     launches_per_step = fwd.launches + (inv.launches if inv else 0)
+    # accuracy of the timed outputs (before anything else reuses the buffers)
+    torch.cuda.synchronize()
+    acc = accuracy(kind, dims, batch, src, mid, back, inv is not None) if rank == 0 else None
 
     # the split-precision tensor-core form on the same workload, same stream
     tc_form = None
@@ -417,6 +450,7 @@ def run_ours(args, cfg):
                      "passes": passes},
         "cpu_baseline": cpu,
         "e2e": e2e,
+        "accuracy": acc,
         "tc_split_form": tc_form,
         "gpu_launches": launches_per_step * args.steps,
         "clocks": dict(clk.summary(), window="soak %.1f s + timed region" % args.soak),
