@@ -302,6 +302,45 @@ def run_queue(args, desc):
     fl = sum(U.flops(k, d) for k, d in items)
     by = sum(U.bytes_moved(k, d) for k, d in items)
     hbm, peak_src = peaks()
+
+    # the split-precision tensor-core form of the same queue on the same data,
+    # and its agreement with the plain FP32 outputs over every transform
+    tc = None
+    if args.form == "plain" and not args.no_tc:
+        snap = buf.clone()
+        qt = G.Queue(U.descs(items, buf, offs), form="tc")
+        for _ in range(3):
+            qt.run(stream)
+        torch.cuda.synchronize()
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for _ in range(args.steps):
+            qt.run(stream)
+        t1.record(stream)
+        torch.cuda.synchronize()
+        ms_tc = t0.elapsed_time(t1) / args.steps
+        nums, dens = [], []
+        for (kind, dims), rec in zip(items, offs):
+            _, o = U.elems(kind, dims)
+            d2 = torch.zeros((), dtype=torch.float64, device=dev)
+            r2 = torch.zeros((), dtype=torch.float64, device=dev)
+            for r in rec[2:]:
+                if r is None:
+                    continue
+                a, b = buf[r:r + o].double(), snap[r:r + o].double()
+                d2 = d2 + ((a - b) ** 2).sum()
+                r2 = r2 + (b ** 2).sum()
+            nums.append(d2)
+            dens.append(r2)
+        num, den = torch.stack(nums), torch.stack(dens)
+        tc = {"value": round(fl / (ms_tc / 1e3) / 1e9, 2), "unit": "GFLOP/s", "ms_per_step": round(ms_tc, 4),
+              "transforms_per_s": round(len(items) / (ms_tc / 1e3), 1), "ratio_to_plain": round(ms / ms_tc, 3),
+              "rel_l2_vs_plain_fp32": float((num.sum() / den.sum()).sqrt()),
+              "max_transform_rel_l2_vs_plain_fp32": float((num / den.clamp_min(1e-300)).sqrt().max()),
+              "launches_per_step": qt.launches,
+              "note": "tcgen05 DFT-16 stages where eligible (radix-16 stages of 256- and 4096-point passes), "
+                      "FP16 hi+lo operands, FP32 accumulation in TMEM; other passes plain FP32"}
+        del qt, snap
     line = {
         "metric": "GFLOP/s (5N·log2N) & HBM GB/s: TC-split+batched vs plain FP32 at rel-L2≤5e-6",
         "value": round(fl / (ms / 1e3) / 1e9, 2), "unit": "GFLOP/s", "n_gpus": 1, "steps": args.steps,
@@ -312,7 +351,7 @@ def run_queue(args, desc):
         "roofline": {"bound": "hbm", "achieved": round(by / (ms / 1e3) / 1e9, 1), "peak": hbm, "unit": "GB/s",
                      "frac": round(by / (ms / 1e3) / 1e9 / hbm, 4), "traffic": args.traffic,
                      "peak_source": peak_src, "kernel": "whole queue (graph of %d launches)" % q.launches},
-        "cpu_baseline": None, "e2e": None, "gpu_launches": q.launches * args.steps,
+        "cpu_baseline": None, "e2e": None, "tc_split_form": tc, "gpu_launches": q.launches * args.steps,
         "clocks": dict(clk.summary(), window="soak %.1f s + timed region" % args.soak),
     }
     print(json.dumps(line), flush=True)
