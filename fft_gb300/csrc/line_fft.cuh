@@ -577,6 +577,73 @@ __device__ __forceinline__ void c2r_paired_body(const LineParams& p, long long c
   else emit(std::false_type{});
 }
 
+// Rows of at most 64 points (T <= 4 threads per line): a warp holds 32/T
+// whole lines, 32 E consecutive elements when the lines are contiguous.
+// Plain 4-byte accesses of the canonical layout touch 8 to 16 lines per warp
+// instruction; staging moves the warp's chunk with coalesced 16-byte accesses
+// through the exchange buffer instead.  Usable when the lines are contiguous
+// (hi == L) and both arrays are 16-byte aligned.
+__device__ __forceinline__ bool rows_contiguous(const LineIO& io, int L) {
+  return io.hi == L && io.qshift == 0 && io.qmask == 0 &&
+         ((reinterpret_cast<uintptr_t>(io.re) | reinterpret_cast<uintptr_t>(io.im)) & 15) == 0;
+}
+
+template <int LOGL, int C, class SM>
+__device__ __forceinline__ void rows_stage_in(const LineParams& p, long long cta, const SM& sm,
+                                              float2 (&v)[Sched<LOGL>::E], int t, int c) {
+  using Sc = Sched<LOGL>;
+  constexpr int L = Sc::L, E = Sc::E, T = Sc::T, WL = 32 / T;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const long long q0 = cta * C + (long long)w * WL;
+  const float4* gr = reinterpret_cast<const float4*>(p.in.re + q0 * L);
+  const float4* gi = reinterpret_cast<const float4*>(p.in.im + q0 * L);
+#pragma unroll
+  for (int i = 0; i < E / 4; i++) {
+    const int f = 32 * i + lane;   // float4 of the warp's chunk
+    const int cl = (4 * f) / L, j = (4 * f) % L;
+    float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
+    if (q0 + cl < p.nlines) {
+      a = __ldg(gr + f);
+      b = __ldg(gi + f);
+    }
+    const int cc = w * WL + cl;
+    sm.put(cc, j, make_float2(a.x, b.x));
+    sm.put(cc, j + 1, make_float2(a.y, b.y));
+    sm.put(cc, j + 2, make_float2(a.z, b.z));
+    sm.put(cc, j + 3, make_float2(a.w, b.w));
+  }
+  __syncwarp();
+#pragma unroll
+  for (int e = 0; e < E; e++) v[e] = sm.get(c, t + T * e);
+  __syncwarp();   // every lane has its values before the stages reuse the buffer
+}
+
+template <int LOGL, int C, class SM>
+__device__ __forceinline__ void rows_stage_out(const LineParams& p, long long cta, const SM& sm,
+                                               const float2 (&v)[Sched<LOGL>::E], int t, int c) {
+  using Sc = Sched<LOGL>;
+  constexpr int L = Sc::L, E = Sc::E, T = Sc::T, WL = 32 / T;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const long long q0 = cta * C + (long long)w * WL;
+  __syncwarp();   // the last stage's reads of the buffer are done
+#pragma unroll
+  for (int e = 0; e < E; e++) sm.put(c, t + T * e, v[e]);
+  __syncwarp();
+  float4* gr = reinterpret_cast<float4*>(p.out.re + q0 * L);
+  float4* gi = reinterpret_cast<float4*>(p.out.im + q0 * L);
+#pragma unroll
+  for (int i = 0; i < E / 4; i++) {
+    const int f = 32 * i + lane;
+    const int cl = (4 * f) / L, j = (4 * f) % L;
+    if (q0 + cl < p.nlines) {
+      const int cc = w * WL + cl;
+      const float2 x0 = sm.get(cc, j), x1 = sm.get(cc, j + 1), x2 = sm.get(cc, j + 2), x3 = sm.get(cc, j + 3);
+      gr[f] = make_float4(x0.x, x1.x, x2.x, x3.x);
+      gi[f] = make_float4(x0.y, x1.y, x2.y, x3.y);
+    }
+  }
+}
+
 // The body of one CTA's work: lines [cta*C, cta*C + C) of the launch `p`.
 // UNIT: both element strides are 1 (split complex rows), so element offsets
 // are compile-time constants instead of runtime 64-bit products.
@@ -641,7 +708,20 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
       for (int e = 0; e < E; e++) v[e] = make_float2(0.f, 0.f);
     }
   } else {
-    if (active) {
+    // short contiguous rows: warp-staged coalesced loads (rows_stage_in)
+    bool staged = false;
+    if constexpr (UNIT && !COLS && T <= 4 && E == 16 && !TC) {
+      if (rows_contiguous(p.in, L)) {
+        rows_stage_in<LOGL, C>(p, cta, sm, v, t, c);
+        if (p.inverse) {
+#pragma unroll
+          for (int e = 0; e < E; e++) v[e] = cswap(v[e]);
+        }
+        staged = true;
+      }
+    }
+    if (staged) {
+    } else if (active) {
       const long long base = line_off(p.in, q);
       if constexpr (UNIT) {
         const float* pr = p.in.re + base + t;
@@ -714,7 +794,14 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
 #pragma unroll
         for (int e = 0; e < E; e++) v[e] = cswap(v[e]);
       }
-      if (active) {
+      bool staged_out = false;
+      if constexpr (UNIT && !COLS && T <= 4 && E == 16 && !TC) {
+        if (rows_contiguous(p.out, L)) {
+          rows_stage_out<LOGL, C>(p, cta, sm, v, t, c);
+          staged_out = true;
+        }
+      }
+      if (!staged_out && active) {
         const long long base = line_off(p.out, q);
         if constexpr (UNIT) {
           float* pr = p.out.re + base + t;
