@@ -577,9 +577,12 @@ __device__ __forceinline__ void c2r_paired_body(const LineParams& p, long long c
   else emit(std::false_type{});
 }
 
-// Rows of at most 64 points (T <= 4 threads per line): a warp holds 32/T
+#ifndef AFFT_STAGE_T
+#define AFFT_STAGE_T 8
+#endif
+// Rows of at most 128 points (T <= 8 threads per line): a warp holds 32/T
 // whole lines, 32 E consecutive elements when the lines are contiguous.
-// Plain 4-byte accesses of the canonical layout touch 8 to 16 lines per warp
+// Plain 4-byte accesses of the canonical layout touch 4 to 32 lines per warp
 // instruction; staging moves the warp's chunk with coalesced 16-byte accesses
 // through the exchange buffer instead.  Usable when the lines are contiguous
 // (hi == L) and both arrays are 16-byte aligned.
@@ -588,12 +591,35 @@ __device__ __forceinline__ bool rows_contiguous(const LineIO& io, int L) {
          ((reinterpret_cast<uintptr_t>(io.re) | reinterpret_cast<uintptr_t>(io.im)) & 15) == 0;
 }
 
+// The staging pass's own view of the exchange buffer and its lane order,
+// chosen by an exhaustive bank count so both the 4-element groups a lane
+// moves and the canonical reads hit distinct bank pairs per half-warp:
+// 32-point lines use pitch 34 with one pad per 16 elements (the stages'
+// layout costs 4x there); 128-point lines keep the stages' layout with lane
+// bits 3 and 4 swapped (2x otherwise).  Warps synchronise only among their
+// own lanes, so each warp's staging view stays inside the region its lines
+// occupy in the stages' layout (WL lines of pitch LP from WL * LP * warp).
+template <int L, class SM>
+__device__ __forceinline__ int stage_idx(const SM& sm, int c, int j) {
+  if constexpr (L == 32) {
+    constexpr int WL = 16;   // lines per warp (2 threads per line)
+    return (c / WL) * (WL * SM::LP) + (c % WL) * 34 + j + (j >> 4);
+  } else {
+    return sm.idx(c, j);
+  }
+}
+template <int L>
+__device__ __forceinline__ int stage_lane(int lane) {
+  if constexpr (L == 128) return (lane & 7) | (((lane >> 3) & 1) << 4) | (((lane >> 4) & 1) << 3);
+  else return lane;
+}
+
 template <int LOGL, int C, class SM>
 __device__ __forceinline__ void rows_stage_in(const LineParams& p, long long cta, const SM& sm,
                                               float2 (&v)[Sched<LOGL>::E], int t, int c) {
   using Sc = Sched<LOGL>;
   constexpr int L = Sc::L, E = Sc::E, T = Sc::T, WL = 32 / T;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int lane = stage_lane<L>(threadIdx.x & 31), w = threadIdx.x >> 5;
   const long long q0 = cta * C + (long long)w * WL;
   const float4* gr = reinterpret_cast<const float4*>(p.in.re + q0 * L);
   const float4* gi = reinterpret_cast<const float4*>(p.in.im + q0 * L);
@@ -607,14 +633,14 @@ __device__ __forceinline__ void rows_stage_in(const LineParams& p, long long cta
       b = __ldg(gi + f);
     }
     const int cc = w * WL + cl;
-    sm.put(cc, j, make_float2(a.x, b.x));
-    sm.put(cc, j + 1, make_float2(a.y, b.y));
-    sm.put(cc, j + 2, make_float2(a.z, b.z));
-    sm.put(cc, j + 3, make_float2(a.w, b.w));
+    sm.s[stage_idx<L>(sm, cc, j)] = make_float2(a.x, b.x);
+    sm.s[stage_idx<L>(sm, cc, j + 1)] = make_float2(a.y, b.y);
+    sm.s[stage_idx<L>(sm, cc, j + 2)] = make_float2(a.z, b.z);
+    sm.s[stage_idx<L>(sm, cc, j + 3)] = make_float2(a.w, b.w);
   }
   __syncwarp();
 #pragma unroll
-  for (int e = 0; e < E; e++) v[e] = sm.get(c, t + T * e);
+  for (int e = 0; e < E; e++) v[e] = sm.s[stage_idx<L>(sm, c, t + T * e)];
   __syncwarp();   // every lane has its values before the stages reuse the buffer
 }
 
@@ -623,11 +649,11 @@ __device__ __forceinline__ void rows_stage_out(const LineParams& p, long long ct
                                                const float2 (&v)[Sched<LOGL>::E], int t, int c) {
   using Sc = Sched<LOGL>;
   constexpr int L = Sc::L, E = Sc::E, T = Sc::T, WL = 32 / T;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int lane = stage_lane<L>(threadIdx.x & 31), w = threadIdx.x >> 5;
   const long long q0 = cta * C + (long long)w * WL;
   __syncwarp();   // the last stage's reads of the buffer are done
 #pragma unroll
-  for (int e = 0; e < E; e++) sm.put(c, t + T * e, v[e]);
+  for (int e = 0; e < E; e++) sm.s[stage_idx<L>(sm, c, t + T * e)] = v[e];
   __syncwarp();
   float4* gr = reinterpret_cast<float4*>(p.out.re + q0 * L);
   float4* gi = reinterpret_cast<float4*>(p.out.im + q0 * L);
@@ -637,7 +663,8 @@ __device__ __forceinline__ void rows_stage_out(const LineParams& p, long long ct
     const int cl = (4 * f) / L, j = (4 * f) % L;
     if (q0 + cl < p.nlines) {
       const int cc = w * WL + cl;
-      const float2 x0 = sm.get(cc, j), x1 = sm.get(cc, j + 1), x2 = sm.get(cc, j + 2), x3 = sm.get(cc, j + 3);
+      const float2 x0 = sm.s[stage_idx<L>(sm, cc, j)], x1 = sm.s[stage_idx<L>(sm, cc, j + 1)],
+                   x2 = sm.s[stage_idx<L>(sm, cc, j + 2)], x3 = sm.s[stage_idx<L>(sm, cc, j + 3)];
       gr[f] = make_float4(x0.x, x1.x, x2.x, x3.x);
       gi[f] = make_float4(x0.y, x1.y, x2.y, x3.y);
     }
@@ -710,7 +737,7 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
   } else {
     // short contiguous rows: warp-staged coalesced loads (rows_stage_in)
     bool staged = false;
-    if constexpr (UNIT && !COLS && T <= 4 && E == 16 && !TC) {
+    if constexpr (UNIT && !COLS && T <= AFFT_STAGE_T && E == 16 && !TC) {
       if (rows_contiguous(p.in, L)) {
         rows_stage_in<LOGL, C>(p, cta, sm, v, t, c);
         if (p.inverse) {
@@ -795,7 +822,7 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
         for (int e = 0; e < E; e++) v[e] = cswap(v[e]);
       }
       bool staged_out = false;
-      if constexpr (UNIT && !COLS && T <= 4 && E == 16 && !TC) {
+      if constexpr (UNIT && !COLS && T <= AFFT_STAGE_T && E == 16 && !TC) {
         if (rows_contiguous(p.out, L)) {
           rows_stage_out<LOGL, C>(p, cta, sm, v, t, c);
           staged_out = true;
