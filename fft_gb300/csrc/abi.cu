@@ -286,6 +286,22 @@ static int check_tc_error(const Plan& P) {
   return 0;
 }
 
+// The data arguments a plan reads and writes: src_re and dst_re always, the
+// im arrays of complex split data.  A missing one is reported, never
+// launched on (a kernel would fault on it).
+static bool data_args(const Plan& P, const float* sr, const float* si, const float* dr, const float* di,
+                      bool* use_si, bool* use_di) {
+  const bool real_in = P.kind == K_R, real_out = P.kind == K_RI;
+  const bool inter = P.format == afft_interleaved;
+  *use_si = !real_in && !inter;
+  *use_di = !real_out && !inter;
+  if (!sr || !dr || (*use_si && !si) || (*use_di && !di)) {
+    set_error(AFFT_GB300_EINVAL, "a data pointer this transform reads or writes is NULL");
+    return false;
+  }
+  return true;
+}
+
 static int transform_sync(void* plan, const float* sr, const float* si, float* dr, float* di) {
   clear_error();
   auto P = lookup(plan);
@@ -295,7 +311,8 @@ static int transform_sync(void* plan, const float* sr, const float* si, float* d
   const bool real_in = P->kind == K_R, real_out = P->kind == K_RI;
   const bool inter = P->format == afft_interleaved;
   // arguments that carry data for this kind/format
-  bool use_si = !real_in && !inter, use_di = !real_out && !inter;
+  bool use_si, use_di;
+  if (!data_args(*P, sr, si, dr, di, &use_si, &use_di)) return AFFT_GB300_EINVAL;
   bool dev = is_device_ptr(sr) && is_device_ptr(dr) && (!use_si || is_device_ptr(si)) &&
              (!use_di || is_device_ptr(di));
   if (dev) {
@@ -510,8 +527,10 @@ int afft_gb300_transform_async(void* plan, const float* sr, const float* si, flo
   if (!P) return AFFT_GB300_ESTATE;
   std::lock_guard<std::mutex> g(P->mu);
   DeviceGuard dg(P->device);
+  bool use_si, use_di;
+  if (!data_args(*P, sr, si, dr, di, &use_si, &use_di)) return AFFT_GB300_EINVAL;
   // NULL is the CUDA default stream, as for a kernel launch
-  return P->launch(sr, si, dr, di, (cudaStream_t)stream);
+  return P->launch(sr, use_si ? si : nullptr, dr, use_di ? di : nullptr, (cudaStream_t)stream);
 }
 
 int afft_gb300_release(void* plan) {

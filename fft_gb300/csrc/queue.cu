@@ -87,6 +87,13 @@ static int build_queue(QueueImpl& Q) {
       set_error(AFFT_GB300_EINVAL, "bad descriptor (kind, ndim 1..3, power-of-two dims)");
       return AFFT_GB300_EINVAL;
     }
+    // split data: src_im for complex input (c, ci, ri), dst_im for complex
+    // output (c, ci, r); a missing array is reported, never launched on
+    const bool cin = d.kind != K_R, cout = d.kind != K_RI;
+    if (!d.src_re || !d.dst_re || (cin && !d.src_im) || (cout && !d.dst_im)) {
+      set_error(AFFT_GB300_EINVAL, "bad descriptor: a data pointer the transform reads or writes is NULL");
+      return AFFT_GB300_EINVAL;
+    }
     std::vector<long long> key{d.kind};
     key.insert(key.end(), dims, dims + nd);
     auto it = Q.plans.find(key);

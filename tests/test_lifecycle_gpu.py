@@ -81,3 +81,37 @@ def test_bounded_wait_reports_timeout(dev):
     yr, yi = np.zeros(256, np.float32), np.zeros(256, np.float32)
     p(x, x, yr, yi)
     assert yr[0] == 256.0 and yi[0] == 256.0
+
+
+def test_missing_data_pointers_are_rejected(dev):
+    # a NULL array the transform reads or writes is reported (EINVAL) before
+    # anything is launched, through the synchronous, async and queue entry
+    # points; the context stays usable
+    L = G.lib()
+    n = 1024
+    x = torch.ones(n, device=dev)
+    y = torch.zeros(n + 2, device=dev)
+    z = torch.zeros(n + 2, device=dev)
+    cases = [
+        (G.complex_transform([n]), (x, None, y, z)),
+        (G.complex_transform([n]), (x, x, None, z)),
+        (G.inverse_complex_transform([n]), (x, x, y, None)),
+        (G.real_transform([n]), (x, None, z)),
+        (G.real_transform([n]), (None, y, z)),
+        (G.inverse_real_transform([n]), (x, None, y)),
+    ]
+    for plan, args in cases:
+        with pytest.raises(G.AfftError):
+            plan(*args)
+        assert G.last_error()[0] == 1
+    p = G.BatchPlan("r", [n], 1)
+    rc = L.afft_gb300_transform_async(p.state, G.ptr(x), None, None, G.ptr(z), None)
+    assert rc == 1
+    with pytest.raises(G.AfftError):
+        G.Queue([("c", [n], x, None, y, z)])
+    # still usable
+    plan = G.complex_transform([n])
+    yr, yi = torch.zeros(n, device=dev), torch.zeros(n, device=dev)
+    plan(x, torch.zeros(n, device=dev), yr, yi)
+    torch.cuda.synchronize()
+    assert abs(float(yr[0]) - n) < 1e-3 and float(yr[1:].abs().max()) < 1e-3
