@@ -739,6 +739,12 @@ static LineIO bind(const IOSpec& s, float* const* base) {
   return o;
 }
 
+bool op_tables_ok(const Op& op) {
+  if (op.type != OP_LINE) return op.type != OP_REAL || op.rp.rtw;
+  return op.p.tw && (op.k.kind == LK_C2C || op.p.rtw) &&
+         (!op.p.tw_n || op.p.tw_full || (op.p.tw_hi && op.p.tw_lo)) && (!op.k.tc || op.p.tc_b);
+}
+
 int Plan::launch(const float* src_re, const float* src_im, float* dst_re, float* dst_im, cudaStream_t st) {
   if (scratch_floats > 0 && !scratch) {
     if (cudaMalloc(&scratch, (size_t)scratch_floats * sizeof(float)) != cudaSuccess) {
@@ -748,6 +754,14 @@ int Plan::launch(const float* src_re, const float* src_im, float* dst_re, float*
     }
   }
   float* base[B_NBUF] = {(float*)src_re, (float*)src_im, dst_re, dst_im, scratch};
+  // every table a line kernel reads must exist: a plan-building mistake is
+  // reported here instead of reaching the GPU as a NULL pointer
+  for (const auto& op : ops) {
+    if (!op_tables_ok(op)) {
+      set_error(4, "plan is missing a twiddle table");
+      return 4;
+    }
+  }
   for (auto& op : ops) {
     if (op.type == OP_LINE) {
       LineParams p = op.p;

@@ -110,6 +110,9 @@ std::unique_ptr<Plan> build_plan(int kind, int ndim, const long long* dims, long
 const __half* tc_matrix_table();
 int* tc_error_word();
 
+// Whether every table an op's kernel reads is present (device plans).
+bool op_tables_ok(const Op& op);
+
 // JSON description of a plan's ops (kernel shapes, grids, address specs).
 std::string describe_plan(const Plan& P);
 

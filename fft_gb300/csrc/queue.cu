@@ -120,6 +120,10 @@ static int build_queue(QueueImpl& Q) {
     const Plan& P = *plan_of[j];
     for (size_t i = 0; i < P.ops.size(); i++) {
       const Op& op = P.ops[i];
+      if (!op_tables_ok(op)) {
+        set_error(AFFT_GB300_ECUDA, "plan is missing a twiddle table");
+        return AFFT_GB300_ECUDA;
+      }
       const void* kid = op.type == OP_LINE ? (const void*)op.k.grouped : (const void*)&elementwise_grouped;
       auto key = std::make_pair((int)i, kid);
       auto it = gidx.find(key);
