@@ -671,6 +671,138 @@ __device__ __forceinline__ void rows_stage_out(const LineParams& p, long long ct
   }
 }
 
+// Short real rows (r2c: L <= 128 complex points of the interleaved view;
+// c2r: L <= 32, measured slower beyond), staged
+// per warp like rows_stage_in/out: the 2L reals of a line are contiguous
+// (float4 accesses, 16-byte aligned), and the L + 1 bins of consecutive
+// lines are contiguous in each split array (coalesced 4-byte accesses, any
+// alignment), kept during staging in a pitch-(L + 1) view inside the warp's
+// region of the exchange buffer.
+__device__ __forceinline__ bool reals_contiguous(const LineIO& io, int L) {
+  return io.es == 2 && io.im == io.re + 1 && io.hi == 2 * L && io.qshift == 0 && io.qmask == 0 &&
+         (reinterpret_cast<uintptr_t>(io.re) & 15) == 0;
+}
+__device__ __forceinline__ bool bins_contiguous(const LineIO& io, int L) {
+  return io.es == 1 && io.hi == L + 1 && io.qshift == 0 && io.qmask == 0;
+}
+template <int L, int WL, class SM>
+__device__ __forceinline__ int bins_idx(int c, int k) {
+  static_assert(L + 1 <= SM::LP, "a line's bins fit its slot of the exchange buffer");
+  return (c / WL) * (WL * SM::LP) + (c % WL) * (L + 1) + k;
+}
+
+// r2c: the interleaved reals of the warp's lines into the canonical layout
+template <int LOGL, int C, class SM>
+__device__ __forceinline__ void rows_stage_in_reals(const LineParams& p, long long cta, const SM& sm,
+                                                    float2 (&v)[Sched<LOGL>::E], int t, int c) {
+  using Sc = Sched<LOGL>;
+  constexpr int L = Sc::L, E = Sc::E, T = Sc::T, WL = 32 / T;
+  const int lane = stage_lane<L>(threadIdx.x & 31), w = threadIdx.x >> 5;
+  const long long q0 = cta * C + (long long)w * WL;
+  const float4* g = reinterpret_cast<const float4*>(p.in.re + q0 * 2 * L);
+#pragma unroll
+  for (int i = 0; i < E / 2; i++) {
+    const int f = 32 * i + lane;   // float4 = 2 complex of the warp's chunk
+    const int cl = (2 * f) / L, j = (2 * f) % L;
+    float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (q0 + cl < p.nlines) a = __ldg(g + f);
+    const int cc = w * WL + cl;
+    sm.s[stage_idx<L>(sm, cc, j)] = make_float2(a.x, a.y);
+    sm.s[stage_idx<L>(sm, cc, j + 1)] = make_float2(a.z, a.w);
+  }
+  __syncwarp();
+#pragma unroll
+  for (int e = 0; e < E; e++) v[e] = sm.s[stage_idx<L>(sm, c, t + T * e)];
+  __syncwarp();
+}
+
+// r2c: the warp's bins X[0..L] (x[e] at k = t + T e, xl = X[L]) out
+template <int LOGL, int C, class SM>
+__device__ __forceinline__ void rows_stage_out_bins(const LineParams& p, long long cta, const SM& sm,
+                                                    const float2 (&x)[Sched<LOGL>::E], float2 xl, int t, int c) {
+  using Sc = Sched<LOGL>;
+  constexpr int L = Sc::L, E = Sc::E, T = Sc::T, WL = 32 / T, B = WL * (L + 1);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const long long q0 = cta * C + (long long)w * WL;
+  __syncwarp();   // the post-pass reads of the buffer are done
+#pragma unroll
+  for (int e = 0; e < E; e++) sm.s[bins_idx<L, WL, SM>(c, t + T * e)] = x[e];
+  if (t == 0) sm.s[bins_idx<L, WL, SM>(c, L)] = xl;
+  __syncwarp();
+  const int wb = bins_idx<L, WL, SM>(w * WL, 0);
+  float* gr = p.out.re + q0 * (L + 1);
+  float* gi = p.out.im + q0 * (L + 1);
+  for (int i = lane; i < B; i += 32) {
+    if (q0 + i / (L + 1) < p.nlines) {
+      const float2 b = sm.s[wb + i];
+      gr[i] = b.x;
+      gi[i] = b.y;
+    }
+  }
+}
+
+// c2r: the warp's bins in, the pre-pass (as in line_fft_body) into the
+// canonical layout
+template <int LOGL, int C, class SM>
+__device__ __forceinline__ void rows_stage_in_bins(const LineParams& p, long long cta, const SM& sm,
+                                                   float2 (&v)[Sched<LOGL>::E], int t, int c) {
+  using Sc = Sched<LOGL>;
+  constexpr int L = Sc::L, E = Sc::E, T = Sc::T, WL = 32 / T, B = WL * (L + 1);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const long long q0 = cta * C + (long long)w * WL;
+  const int wb = bins_idx<L, WL, SM>(w * WL, 0);
+  const float* gr = p.in.re + q0 * (L + 1);
+  const float* gi = p.in.im + q0 * (L + 1);
+  for (int i = lane; i < B; i += 32) {
+    float2 b = make_float2(0.f, 0.f);
+    if (q0 + i / (L + 1) < p.nlines) b = make_float2(__ldg(gr + i), __ldg(gi + i));
+    sm.s[wb + i] = b;
+  }
+  __syncwarp();
+#pragma unroll
+  for (int e = 0; e < E; e++) {
+    const int i = t + T * e;
+    const float2 s0 = sm.s[bins_idx<L, WL, SM>(c, i)];
+    const float2 s1 = sm.s[bins_idx<L, WL, SM>(c, L - i)];
+    float2 z;
+    if (i == 0) {
+      z = make_float2(s0.x + s1.x, s0.x - s1.x);
+    } else {
+      const float2 wt = ldg2(p.rtw + i);
+      const float2 a = cadd(s0, cconj(s1));
+      const float2 b = cmul(csub(cconj(s1), s0), cconj(wt));
+      z = cadd(a, cmul_negi(b));
+    }
+    v[e] = cswap(z);
+  }
+  __syncwarp();
+}
+
+// c2r: the canonical outputs z (reals x[2k], x[2k+1]) out as float4
+template <int LOGL, int C, class SM>
+__device__ __forceinline__ void rows_stage_out_reals(const LineParams& p, long long cta, const SM& sm,
+                                                     const float2 (&z)[Sched<LOGL>::E], int t, int c) {
+  using Sc = Sched<LOGL>;
+  constexpr int L = Sc::L, E = Sc::E, T = Sc::T, WL = 32 / T;
+  const int lane = stage_lane<L>(threadIdx.x & 31), w = threadIdx.x >> 5;
+  const long long q0 = cta * C + (long long)w * WL;
+  __syncwarp();   // the last stage's reads of the buffer are done
+#pragma unroll
+  for (int e = 0; e < E; e++) sm.s[stage_idx<L>(sm, c, t + T * e)] = z[e];
+  __syncwarp();
+  float4* g = reinterpret_cast<float4*>(p.out.re + q0 * 2 * L);
+#pragma unroll
+  for (int i = 0; i < E / 2; i++) {
+    const int f = 32 * i + lane;
+    const int cl = (2 * f) / L, j = (2 * f) % L;
+    if (q0 + cl < p.nlines) {
+      const int cc = w * WL + cl;
+      const float2 z0 = sm.s[stage_idx<L>(sm, cc, j)], z1 = sm.s[stage_idx<L>(sm, cc, j + 1)];
+      g[f] = make_float4(z0.x, z0.y, z1.x, z1.y);
+    }
+  }
+}
+
 // The body of one CTA's work: lines [cta*C, cta*C + C) of the launch `p`.
 // UNIT: both element strides are 1 (split complex rows), so element offsets
 // are compile-time constants instead of runtime 64-bit products.
@@ -710,7 +842,16 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
     // inverse): Z'[i] = a - i*b, a = X[i] + conj(X[L-i]),
     // b = (conj(X[L-i]) - X[i]) * conj(w_i); Z'[0] from the real parts of
     // X[0] and X[L]; then the inverse transform of Z' (swap trick).
-    if (active) {
+    bool staged = false;
+    // (lines of at most 32 points: at 128 points staging measured 1.4x slower)
+    if constexpr (!COLS && T <= 2 && E == 16 && !TC) {
+      if (bins_contiguous(p.in, L)) {
+        rows_stage_in_bins<LOGL, C>(p, cta, sm, v, t, c);
+        staged = true;
+      }
+    }
+    if (staged) {
+    } else if (active) {
       const long long base = line_off(p.in, q);
 #pragma unroll
       for (int e = 0; e < E; e++) {
@@ -737,6 +878,12 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
   } else {
     // short contiguous rows: warp-staged coalesced loads (rows_stage_in)
     bool staged = false;
+    if constexpr (KIND == LK_R2C && !COLS && T <= AFFT_STAGE_T && E == 16 && !TC) {
+      if (reals_contiguous(p.in, L)) {
+        rows_stage_in_reals<LOGL, C>(p, cta, sm, v, t, c);
+        staged = true;
+      }
+    }
     if constexpr (UNIT && !COLS && T <= AFFT_STAGE_T && E == 16 && !TC) {
       if (rows_contiguous(p.in, L)) {
         rows_stage_in<LOGL, C>(p, cta, sm, v, t, c);
@@ -849,14 +996,22 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
       }
     }
   } else if constexpr (KIND == LK_C2R) {
-    if (active) {
+#pragma unroll
+    for (int e = 0; e < E; e++) v[e] = cswap(v[e]);
+    bool staged_out = false;
+    if constexpr (!COLS && T <= 2 && E == 16 && !TC) {
+      if (reals_contiguous(p.out, L)) {
+        rows_stage_out_reals<LOGL, C>(p, cta, sm, v, t, c);
+        staged_out = true;
+      }
+    }
+    if (!staged_out && active) {
       const long long base = line_off(p.out, q);
 #pragma unroll
       for (int e = 0; e < E; e++) {
-        const float2 z = cswap(v[e]);
         const long long a = base + (long long)(t + T * e) * p.out.es;
-        p.out.re[a] = z.x;
-        p.out.im[a] = z.y;
+        p.out.re[a] = v[e].x;
+        p.out.im[a] = v[e].y;
       }
     }
   } else {
@@ -867,29 +1022,71 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
 #pragma unroll
     for (int e = 0; e < E; e++) sm.put(c, t + T * e, v[e]);
     line_sync<WARP_ONLY>();
-    if (active) {
-      const long long base = line_off(p.out, q);
+    if constexpr (!COLS && T <= AFFT_STAGE_T && E == 16 && !TC) {
+      // bins X[k] (k = t + T e) replace v; xl = X[L] (from the k = 0 thread)
+      float2 xl = make_float2(0.f, 0.f);
 #pragma unroll
       for (int e = 0; e < E; e++) {
         const int k = t + T * e;
         const float2 s0 = v[e];
         const float2 s1 = sm.get(c, (L - k) & (L - 1));
-        float2 x;
         if (k == 0) {
-          x = make_float2(s0.x + s0.y, 0.f);
-          const long long aL = base + (long long)L * p.out.es;
-          p.out.re[aL] = s0.x - s0.y;
-          p.out.im[aL] = 0.f;
+          v[e] = make_float2(s0.x + s0.y, 0.f);
+          xl = make_float2(s0.x - s0.y, 0.f);
         } else {
           const float2 w = ldg2(p.rtw + k);
           const float2 a = make_float2(0.5f * (s0.x + s1.x), 0.5f * (s0.y - s1.y));
           const float2 d = make_float2(0.5f * (s0.x - s1.x), 0.5f * (s0.y + s1.y));
           const float2 b = cmul(d, w);
-          x = cadd(a, cmul_negi(b));
+          v[e] = cadd(a, cmul_negi(b));
         }
-        const long long a = base + (long long)k * p.out.es;
-        p.out.re[a] = x.x;
-        p.out.im[a] = x.y;
+      }
+      bool staged_out = false;
+      if constexpr (!COLS && T <= AFFT_STAGE_T && E == 16 && !TC) {
+        if (bins_contiguous(p.out, L)) {
+          rows_stage_out_bins<LOGL, C>(p, cta, sm, v, xl, t, c);
+          staged_out = true;
+        }
+      }
+      if (!staged_out && active) {
+        const long long base = line_off(p.out, q);
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+          const long long a = base + (long long)(t + T * e) * p.out.es;
+          p.out.re[a] = v[e].x;
+          p.out.im[a] = v[e].y;
+        }
+        if (t == 0) {
+          const long long aL = base + (long long)L * p.out.es;
+          p.out.re[aL] = xl.x;
+          p.out.im[aL] = xl.y;
+        }
+      }
+    } else {
+      if (active) {
+        const long long base = line_off(p.out, q);
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+          const int k = t + T * e;
+          const float2 s0 = v[e];
+          const float2 s1 = sm.get(c, (L - k) & (L - 1));
+          float2 x;
+          if (k == 0) {
+            x = make_float2(s0.x + s0.y, 0.f);
+            const long long aL = base + (long long)L * p.out.es;
+            p.out.re[aL] = s0.x - s0.y;
+            p.out.im[aL] = 0.f;
+          } else {
+            const float2 w = ldg2(p.rtw + k);
+            const float2 a = make_float2(0.5f * (s0.x + s1.x), 0.5f * (s0.y - s1.y));
+            const float2 d = make_float2(0.5f * (s0.x - s1.x), 0.5f * (s0.y + s1.y));
+            const float2 b = cmul(d, w);
+            x = cadd(a, cmul_negi(b));
+          }
+          const long long a = base + (long long)k * p.out.es;
+          p.out.re[a] = x.x;
+          p.out.im[a] = x.y;
+        }
       }
     }
   }

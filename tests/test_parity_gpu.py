@@ -500,3 +500,49 @@ def test_caller_device_unchanged(dev):
     x = np.ones(256, np.float32)
     p(x, x, np.zeros(256, np.float32), np.zeros(256, np.float32))
     assert torch.cuda.current_device() == 0
+
+
+@pytest.mark.parametrize("kind", ["r", "ri"])
+@pytest.mark.parametrize("n", [32, 64, 128, 256, 512])
+@pytest.mark.parametrize("batch", [1, 7, 1000, 4099])
+@pytest.mark.parametrize("fmt,pad", [(G.afft_split, 0), (G.afft_interleaved, 0), (G.afft_split, 1)],
+                         ids=["split", "inter", "split-offset"])
+def test_batched_small_real(kind, n, batch, fmt, pad, dev):
+    # many short real transforms per CTA: batches that leave warps and CTAs
+    # partly filled, both formats, and arrays that start off 16-byte alignment
+    h = n // 2 + 1
+    rng = np.random.default_rng(n * 7 + batch)
+    inter = fmt == G.afft_interleaved
+    p = G.BatchPlan(kind, [n], batch, fmt=fmt)
+    dvec = lambda x: to_dev(x, dev, pad)
+    if kind == "r":
+        a = rng.standard_normal(n * batch).astype(np.float32)
+        if inter:
+            d = torch.zeros(2 * h * batch + pad + 1, device=dev)[pad:pad + 2 * h * batch]
+            p(dvec(a), d)
+            o = d.cpu().numpy()
+            got = (o[0::2], o[1::2])
+        else:
+            dr = torch.zeros(h * batch + pad + 1, device=dev)[pad:pad + h * batch]
+            di = torch.zeros(h * batch + pad + 1, device=dev)[pad:pad + h * batch]
+            p(dvec(a), dr, di)
+            got = (dr.cpu().numpy(), di.cpu().numpy())
+        for t in sorted({0, batch // 2, batch - 1}):
+            ref = O.oracle64("r", [n], a[t * n:(t + 1) * n])
+            sl = slice(t * h, (t + 1) * h)
+            assert O.rel_l2((got[0][sl], got[1][sl]), ref) <= TOL, (n, batch, t)
+    else:
+        xr = rng.standard_normal(h * batch).astype(np.float32)
+        xi = rng.standard_normal(h * batch).astype(np.float32)
+        d = torch.zeros(n * batch + pad + 1, device=dev)[pad:pad + n * batch]
+        if inter:
+            src = np.empty(2 * h * batch, np.float32)
+            src[0::2], src[1::2] = xr, xi
+            p(dvec(src), None, d)
+        else:
+            p(dvec(xr), dvec(xi), d)
+        got = d.cpu().numpy()
+        for t in sorted({0, batch // 2, batch - 1}):
+            sl = slice(t * h, (t + 1) * h)
+            ref = O.oracle64("ri", [n], xr[sl], xi[sl])
+            assert O.rel_l2(got[t * n:(t + 1) * n], ref) <= TOL, (n, batch, t)
