@@ -580,6 +580,9 @@ __device__ __forceinline__ void c2r_paired_body(const LineParams& p, long long c
 #ifndef AFFT_STAGE_T
 #define AFFT_STAGE_T 8
 #endif
+#ifndef AFFT_C2R_OUT_T
+#define AFFT_C2R_OUT_T 8
+#endif
 // Rows of at most 128 points (T <= 8 threads per line): a warp holds 32/T
 // whole lines, 32 E consecutive elements when the lines are contiguous.
 // Plain 4-byte accesses of the canonical layout touch 4 to 32 lines per warp
@@ -672,7 +675,8 @@ __device__ __forceinline__ void rows_stage_out(const LineParams& p, long long ct
 }
 
 // Short real rows (r2c: L <= 128 complex points of the interleaved view;
-// c2r: L <= 32, measured slower beyond), staged
+// c2r: input for L <= 32, measured slower beyond, output for L <= 128),
+// staged
 // per warp like rows_stage_in/out: the 2L reals of a line are contiguous
 // (float4 accesses, 16-byte aligned), and the L + 1 bins of consecutive
 // lines are contiguous in each split array (coalesced 4-byte accesses, any
@@ -999,7 +1003,7 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
 #pragma unroll
     for (int e = 0; e < E; e++) v[e] = cswap(v[e]);
     bool staged_out = false;
-    if constexpr (!COLS && T <= 2 && E == 16 && !TC) {
+    if constexpr (!COLS && T <= AFFT_C2R_OUT_T && E == 16 && !TC) {
       if (reals_contiguous(p.out, L)) {
         rows_stage_out_reals<LOGL, C>(p, cta, sm, v, t, c);
         staged_out = true;
