@@ -16,7 +16,7 @@ struct LineKernel {
   int kind;            // LK_C2C / LK_R2C / LK_C2R
   int tstore;          // store with the along-line mapping (four-step pass A)
   int tc;              // split-precision tensor-core butterflies
-  int unit;            // unit element strides specialised (rows c2c)
+  int unit;            // unit element strides specialised (rows c2c): 1 split, 2 interleaved
   int lines_per_cta;   // C
   int threads;         // T * C
   size_t smem;         // bytes of dynamic shared memory
@@ -31,6 +31,8 @@ constexpr int COLS_MAX_LOG = 11;   // cols mode: one CTA up to 2048 points
 bool get_line_kernel(int logl, bool cols, int kind, bool tstore, LineKernel* out);
 // rows c2c with unit element strides (split data): compile-time offsets
 bool get_rows_c2c_unit(int logl, bool tc, LineKernel* out);
+// rows c2c on interleaved pairs with unit pair strides (float2 accesses)
+bool get_rows_c2c_iunit(int logl, LineKernel* out);
 
 // split-precision tensor-core form: rows c2c L = 256 or 4096, cols c2c L = 256
 bool get_tc_kernel(int logl, bool cols, bool tstore, LineKernel* out);
@@ -62,7 +64,7 @@ constexpr int lines_per_cta_k() {
   return KIND == LK_R2C_HALF ? AFFT_HALF_C : lines_per_cta<LOGL, COLS>();
 }
 
-template <int LOGL, bool COLS, int KIND, bool TSTORE, bool TC = false, bool UNIT = false>
+template <int LOGL, bool COLS, int KIND, bool TSTORE, bool TC = false, int UNIT = 0>
 LineKernel make_line_kernel() {
   constexpr int C = lines_per_cta_k<LOGL, COLS, KIND>();
   constexpr int L = 1 << LOGL;

@@ -808,9 +808,11 @@ __device__ __forceinline__ void rows_stage_out_reals(const LineParams& p, long l
 }
 
 // The body of one CTA's work: lines [cta*C, cta*C + C) of the launch `p`.
-// UNIT: both element strides are 1 (split complex rows), so element offsets
-// are compile-time constants instead of runtime 64-bit products.
-template <int LOGL, int C, bool COLS, int KIND, bool TSTORE, bool TC = false, bool UNIT = false>
+// UNIT: 1 both element strides are 1 (split complex rows), 2 both are 2 with
+// im = re + 1 (interleaved complex rows, loaded and stored as float2), so
+// element offsets are compile-time constants instead of runtime 64-bit
+// products.
+template <int LOGL, int C, bool COLS, int KIND, bool TSTORE, bool TC = false, int UNIT = 0>
 __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta, TcState* ts = nullptr) {
   if constexpr (KIND == LK_R2C_HALF) {
     static_assert(COLS && !TSTORE && !TC, "the split R2C pass is a plain cols pass");
@@ -888,24 +890,42 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
         staged = true;
       }
     }
-    if constexpr (UNIT && !COLS && T <= AFFT_STAGE_T && E == 16 && !TC) {
+    if constexpr (UNIT == 1 && !COLS && T <= AFFT_STAGE_T && E == 16 && !TC) {
       if (rows_contiguous(p.in, L)) {
         rows_stage_in<LOGL, C>(p, cta, sm, v, t, c);
-        if (p.inverse) {
-#pragma unroll
-          for (int e = 0; e < E; e++) v[e] = cswap(v[e]);
-        }
         staged = true;
+      }
+    }
+    if constexpr (UNIT == 2 && !COLS && T <= AFFT_STAGE_T && E == 16 && !TC) {
+      if (reals_contiguous(p.in, L)) {   // interleaved pairs: the same view as real rows
+        rows_stage_in_reals<LOGL, C>(p, cta, sm, v, t, c);
+        staged = true;
+      }
+    }
+    if constexpr (UNIT != 0) {
+      if (staged && p.inverse) {
+#pragma unroll
+        for (int e = 0; e < E; e++) v[e] = cswap(v[e]);
       }
     }
     if (staged) {
     } else if (active) {
       const long long base = line_off(p.in, q);
-      if constexpr (UNIT) {
+      if constexpr (UNIT == 1) {
         const float* pr = p.in.re + base + t;
         const float* pi = p.in.im + base + t;
 #pragma unroll
         for (int e = 0; e < E; e++) v[e] = make_float2(__ldg(pr + T * e), __ldg(pi + T * e));
+      } else if constexpr (UNIT == 2) {
+        const float* pz = p.in.re + base;
+        if ((reinterpret_cast<uintptr_t>(pz) & 7) == 0) {
+          const float2* pp = reinterpret_cast<const float2*>(pz) + t;
+#pragma unroll
+          for (int e = 0; e < E; e++) v[e] = __ldg(pp + T * e);
+        } else {
+#pragma unroll
+          for (int e = 0; e < E; e++) v[e] = make_float2(__ldg(pz + 2 * (t + T * e)), __ldg(pz + 2 * (t + T * e) + 1));
+        }
       } else {
 #pragma unroll
         for (int e = 0; e < E; e++) {
@@ -973,21 +993,40 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
         for (int e = 0; e < E; e++) v[e] = cswap(v[e]);
       }
       bool staged_out = false;
-      if constexpr (UNIT && !COLS && T <= AFFT_STAGE_T && E == 16 && !TC) {
+      if constexpr (UNIT == 1 && !COLS && T <= AFFT_STAGE_T && E == 16 && !TC) {
         if (rows_contiguous(p.out, L)) {
           rows_stage_out<LOGL, C>(p, cta, sm, v, t, c);
           staged_out = true;
         }
       }
+      if constexpr (UNIT == 2 && !COLS && T <= AFFT_STAGE_T && E == 16 && !TC) {
+        if (reals_contiguous(p.out, L)) {
+          rows_stage_out_reals<LOGL, C>(p, cta, sm, v, t, c);
+          staged_out = true;
+        }
+      }
       if (!staged_out && active) {
         const long long base = line_off(p.out, q);
-        if constexpr (UNIT) {
+        if constexpr (UNIT == 1) {
           float* pr = p.out.re + base + t;
           float* pi = p.out.im + base + t;
 #pragma unroll
           for (int e = 0; e < E; e++) {
             pr[T * e] = v[e].x;
             pi[T * e] = v[e].y;
+          }
+        } else if constexpr (UNIT == 2) {
+          float* pz = p.out.re + base;
+          if ((reinterpret_cast<uintptr_t>(pz) & 7) == 0) {
+            float2* pp = reinterpret_cast<float2*>(pz) + t;
+#pragma unroll
+            for (int e = 0; e < E; e++) pp[T * e] = v[e];
+          } else {
+#pragma unroll
+            for (int e = 0; e < E; e++) {
+              pz[2 * (t + T * e)] = v[e].x;
+              pz[2 * (t + T * e) + 1] = v[e].y;
+            }
           }
         } else {
 #pragma unroll
@@ -1136,7 +1175,7 @@ __device__ __forceinline__ void tc_teardown(const TcState& S) {
   if (threadIdx.x < 32) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(S.tmem), "n"(COLS));
 }
 
-template <int LOGL, int C, bool COLS, int KIND, bool TSTORE, bool TC = false, bool UNIT = false>
+template <int LOGL, int C, bool COLS, int KIND, bool TSTORE, bool TC = false, int UNIT = 0>
 __global__ void __launch_bounds__(Sched<LOGL>::T * C, min_ctas<Sched<LOGL>::T * C>())
 line_fft(const LineParams p) {
   if constexpr (TC) {
@@ -1174,7 +1213,7 @@ __device__ __forceinline__ void stage_params(LineParams& dst, const LineParams& 
   }
 }
 
-template <int LOGL, int C, bool COLS, int KIND, bool TSTORE, bool TC = false, bool UNIT = false>
+template <int LOGL, int C, bool COLS, int KIND, bool TSTORE, bool TC = false, int UNIT = 0>
 __global__ void __launch_bounds__(Sched<LOGL>::T * C, min_ctas<Sched<LOGL>::T * C>())
 line_fft_grouped(const Segment* __restrict__ segs, const int* __restrict__ seg_of, long long total) {
   __shared__ LineParams sp;

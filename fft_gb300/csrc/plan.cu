@@ -318,8 +318,13 @@ struct Builder {
     op.type = OP_LINE;
     bool tc = P.form == FORM_TC && kind == LK_C2C && get_tc_kernel(logl, cols, tstore, &op.k);
     const bool unit = !cols && !tstore && kind == LK_C2C && in.es == 1 && out.es == 1;
+    // interleaved pairs (im right after re in the same array) with unit pair strides
+    auto pairs = [](const IOSpec& v) { return v.es == 2 && v.re.buf == v.im.buf && v.im.off == v.re.off + 1; };
+    const bool iunit = !cols && !tstore && kind == LK_C2C && !tc && pairs(in) && pairs(out);
     if (unit && get_rows_c2c_unit(logl, tc, &op.k)) {
       // same kernel with compile-time element offsets
+    } else if (iunit && get_rows_c2c_iunit(logl, &op.k)) {
+      // the same on interleaved pairs
     } else if (!tc && !get_line_kernel(logl, cols, kind, tstore, &op.k)) {
       fail("no kernel for this line length");
       return;

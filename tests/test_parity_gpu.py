@@ -546,3 +546,25 @@ def test_batched_small_real(kind, n, batch, fmt, pad, dev):
             sl = slice(t * h, (t + 1) * h)
             ref = O.oracle64("ri", [n], xr[sl], xi[sl])
             assert O.rel_l2(got[t * n:(t + 1) * n], ref) <= TOL, (n, batch, t)
+
+
+@pytest.mark.parametrize("kind", ["c", "ci"])
+@pytest.mark.parametrize("n", [16, 64, 128, 1024, 4096])
+@pytest.mark.parametrize("batch", [1, 7, 1000])
+@pytest.mark.parametrize("pad", [0, 1, 2], ids=["aligned16", "offset4", "offset8"])
+def test_batched_interleaved_complex(kind, n, batch, pad, dev):
+    # interleaved pairs: float2 accesses when 8-byte aligned, float4 staging
+    # for short lines when 16-byte aligned, scalar accesses otherwise
+    rng = np.random.default_rng(n + batch + pad)
+    a = rng.standard_normal(n * batch).astype(np.float32)
+    b = rng.standard_normal(n * batch).astype(np.float32)
+    src = np.empty(2 * n * batch, np.float32)
+    src[0::2], src[1::2] = a, b
+    p = G.BatchPlan(kind, [n], batch, fmt=G.afft_interleaved)
+    d = torch.zeros(2 * n * batch + pad + 1, device=dev)[pad:pad + 2 * n * batch]
+    p(to_dev(src, dev, pad), None, d, None)
+    o = d.cpu().numpy()
+    for t in sorted({0, batch // 2, batch - 1}):
+        sl = slice(t * n, (t + 1) * n)
+        ref = O.oracle64(kind, [n], a[sl], b[sl])
+        assert O.rel_l2((o[0::2][sl], o[1::2][sl]), ref) <= TOL, (kind, n, batch, pad, t)
