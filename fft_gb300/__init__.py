@@ -24,6 +24,7 @@ afft_auto, afft_scalar, afft_sse2, afft_avx2, afft_avx512f, afft_neon, afft_gb30
 afft_split, afft_interleaved = 0, 1
 KIND_C, KIND_CI, KIND_R, KIND_RI = 0, 1, 2, 3
 FORM_TC = 0x100   # AFFT_GB300_FORM_TC: split-precision tensor-core butterflies
+FORM_F64 = 0x200  # AFFT_GB300_FORM_F64: FP64 data and arithmetic (the afft_64_* path)
 KINDS = {"c": KIND_C, "ci": KIND_CI, "r": KIND_R, "ri": KIND_RI}
 ERRORS = {0: "OK", 1: "EINVAL", 2: "ENODEV", 3: "ENOMEM", 4: "ECUDA", 5: "ESTATE", 6: "ETIMEOUT"}
 
@@ -222,28 +223,33 @@ def half_elems(dims):
 
 
 class _Plan:
-    """A plan placement-built into caller-owned memory (fft.hpp:8-47)."""
+    """A plan placement-built into caller-owned memory (fft.hpp:8-47).
+    ``bits`` selects the afft_32_* (float) or afft_64_* (double) entry points,
+    as fft.hpp's class templates do for T = float / double."""
 
     kind = None
 
-    def __init__(self, dims, mem=None, impl=afft_auto, fmt=afft_split):
+    def __init__(self, dims, mem=None, impl=afft_auto, fmt=afft_split, bits=32):
         L = lib()
+        if bits not in (32, 64):
+            raise ValueError("bits must be 32 or 64")
         self.dims = [int(d) for d in dims]
         self.format = fmt
+        self.bits = bits
         arr, n = _dims(self.dims)
         name = {KIND_C: "c", KIND_CI: "ci", KIND_R: "r", KIND_RI: "ri"}[self.kind]
-        size = getattr(L, "afft_32_%s_memsize" % name)(n, arr, fmt, impl)
+        size = getattr(L, "afft_%d_%s_memsize" % (bits, name))(n, arr, fmt, impl)
         self._mem = None
         self.state = None
         if size == 0 or size == ctypes.c_size_t(-1).value:
             _check("memsize")
             raise AfftError("memsize rejected the plan")
         self._mem = mem if mem is not None else ctypes.create_string_buffer(size)
-        self.state = getattr(L, "afft_32_%s_create" % name)(n, arr, fmt, ctypes.addressof(self._mem), impl)
+        self.state = getattr(L, "afft_%d_%s_create" % (bits, name))(n, arr, fmt, ctypes.addressof(self._mem), impl)
         if not self.state:
             _check("create")
             raise AfftError("create failed")
-        self._fn = getattr(L, "afft_32_%s_transform" % name)
+        self._fn = getattr(L, "afft_%d_%s_transform" % (bits, name))
 
     def __bool__(self):
         return bool(self.state)
@@ -299,8 +305,10 @@ class inverse_real_transform(_Plan):
 class BatchPlan:
     """``batch`` dense transforms of one shape and kind (extension).
 
-    ``__call__`` is synchronous (like afft); ``launch`` enqueues on a CUDA
-    stream (device pointers only) and returns immediately.
+    ``form``: None / "plain" (FP32), "tc" (split-precision tensor cores) or
+    "f64" (double arrays, FP64 arithmetic).  ``__call__`` is synchronous (like
+    afft); ``launch`` enqueues on a CUDA stream (device pointers only) and
+    returns immediately.
     """
 
     def __init__(self, kind, dims, batch, fmt=afft_split, form=None):
@@ -312,8 +320,10 @@ class BatchPlan:
         self.form = form
         if form == "tc":
             fmt = fmt | FORM_TC
+        elif form == "f64":
+            fmt = fmt | FORM_F64
         elif form not in (None, "plain"):
-            raise ValueError("form must be None, 'plain' or 'tc'")
+            raise ValueError("form must be None, 'plain', 'tc' or 'f64'")
         arr, n = _dims(self.dims)
         size = L.afft_gb300_batch_memsize(self.kind, n, arr, self.batch, fmt)
         self.state = None
@@ -326,7 +336,7 @@ class BatchPlan:
             _check("batch_create")
             raise AfftError("batch_create failed")
         name = {KIND_C: "c", KIND_CI: "ci", KIND_R: "r", KIND_RI: "ri"}[self.kind]
-        self._fn = getattr(L, "afft_32_%s_transform" % name)
+        self._fn = getattr(L, "afft_%d_%s_transform" % (64 if form == "f64" else 32, name))
 
     def __call__(self, a, b=None, c=None, d=None):
         if self.kind in (KIND_C, KIND_CI):

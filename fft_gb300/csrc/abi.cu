@@ -162,8 +162,7 @@ static void* create_impl(int kind, size_t ndim, const size_t* dim, size_t batch,
   if (!P) return nullptr;
   // device scratch now, so later launches allocate nothing (and can be
   // captured into CUDA graphs)
-  if (P->scratch_floats > 0 &&
-      cudaMalloc(&P->scratch, (size_t)P->scratch_floats * sizeof(float)) != cudaSuccess) {
+  if (P->scratch_elems > 0 && cudaMalloc(&P->scratch, (size_t)P->scratch_elems * P->esize()) != cudaSuccess) {
     cudaGetLastError();
     set_error(AFFT_GB300_ENOMEM, "scratch allocation failed");
     return nullptr;
@@ -302,10 +301,17 @@ static bool data_args(const Plan& P, const float* sr, const float* si, const flo
   return true;
 }
 
-static int transform_sync(void* plan, const float* sr, const float* si, float* dr, float* di) {
+// f64: the call is one of the afft_64_* transforms (data are doubles, passed
+// here as float pointers); a plan of the other precision is refused.
+static int transform_sync(void* plan, const float* sr, const float* si, float* dr, float* di, bool f64 = false) {
   clear_error();
   auto P = lookup(plan);
   if (!P) return AFFT_GB300_ESTATE;
+  if (P->f64() != f64) {
+    set_error(AFFT_GB300_EINVAL, f64 ? "an FP32 plan passed to an afft_64 transform"
+                                     : "an FP64 plan passed to an afft_32 transform");
+    return AFFT_GB300_EINVAL;
+  }
   std::lock_guard<std::mutex> g(P->mu);
   DeviceGuard dg(P->device);
   const bool real_in = P->kind == K_R, real_out = P->kind == K_RI;
@@ -346,9 +352,10 @@ static int transform_sync(void* plan, const float* sr, const float* si, float* d
   // copy of chunk i-1 out overlap (three streams, ordered by events).
   long long in_n, out_n;
   io_elems(*P, &in_n, &out_n);
-  size_t fin = (size_t)in_n * (inter && !real_in ? 2 : 1);   // floats of src_re
-  size_t fout = (size_t)out_n * (inter && !real_out ? 2 : 1);
-  size_t need = (fin + (use_si ? fin : 0) + fout + (use_di ? fout : 0)) * sizeof(float);
+  const size_t esz = P->esize();
+  const size_t fin = (size_t)in_n * (inter && !real_in ? 2 : 1) * esz;   // bytes of src_re
+  const size_t fout = (size_t)out_n * (inter && !real_out ? 2 : 1) * esz;
+  const size_t need = fin + (use_si ? fin : 0) + fout + (use_di ? fout : 0);
   if (P->stage_bytes < need) {
     if (P->stage) cudaFree(P->stage);
     P->stage = nullptr;
@@ -360,10 +367,14 @@ static int transform_sync(void* plan, const float* sr, const float* si, float* d
     }
     P->stage_bytes = need;
   }
-  float* d_sr = P->stage;
-  float* d_si = use_si ? d_sr + fin : nullptr;
-  float* d_dr = d_sr + fin + (use_si ? fin : 0);
-  float* d_di = use_di ? d_dr + fout : nullptr;
+  char* d_sr = reinterpret_cast<char*>(P->stage);
+  char* d_si = use_si ? d_sr + fin : nullptr;
+  char* d_dr = d_sr + fin + (use_si ? fin : 0);
+  char* d_di = use_di ? d_dr + fout : nullptr;
+  const char* h_sr = reinterpret_cast<const char*>(sr);
+  const char* h_si = reinterpret_cast<const char*>(si);
+  char* h_dr = reinterpret_cast<char*>(dr);
+  char* h_di = reinterpret_cast<char*>(di);
   if (!P->copy_in) {
     // chunking: the largest divisor of the batch up to 8, for batches whose
     // data is worth overlapping (>= 8 MiB)
@@ -372,7 +383,7 @@ static int transform_sync(void* plan, const float* sr, const float* si, float* d
       for (long long d = 8; d >= 2; d--)
         if (P->batch % d == 0) { k = d; break; }
     if (k > 1) {
-      P->chunk = build_plan(P->kind, P->ndim, P->dims, P->batch / k, P->format);
+      P->chunk = build_plan(P->kind, P->ndim, P->dims, P->batch / k, P->format, false, P->form);
       if (!P->chunk) k = 1;
     }
     P->nchunks = k;
@@ -386,22 +397,23 @@ static int transform_sync(void* plan, const float* sr, const float* si, float* d
     for (auto& e : P->ev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
   }
   const long long k = P->nchunks;
-  const size_t cin = fin / k, cout = fout / k;    // floats per chunk, per array
+  const size_t cin = fin / k, cout = fout / k;    // bytes per chunk, per array
+  auto f = [](char* p) { return reinterpret_cast<float*>(p); };
   for (long long i = 0; i < k; i++) {
-    cudaMemcpyAsync(d_sr + i * cin, sr + i * cin, cin * sizeof(float), cudaMemcpyDefault, P->copy_in);
-    if (use_si) cudaMemcpyAsync(d_si + i * cin, si + i * cin, cin * sizeof(float), cudaMemcpyDefault, P->copy_in);
+    cudaMemcpyAsync(d_sr + i * cin, h_sr + i * cin, cin, cudaMemcpyDefault, P->copy_in);
+    if (use_si) cudaMemcpyAsync(d_si + i * cin, h_si + i * cin, cin, cudaMemcpyDefault, P->copy_in);
     cudaEventRecord(P->ev[2 * i], P->copy_in);
   }
   Plan& C = k > 1 ? *P->chunk : *P;
   for (long long i = 0; i < k; i++) {
     cudaStreamWaitEvent(P->stream, P->ev[2 * i], 0);
-    int rc = C.launch(d_sr + i * cin, use_si ? d_si + i * cin : nullptr, d_dr + i * cout,
-                      use_di ? d_di + i * cout : nullptr, P->stream);
+    int rc = C.launch(f(d_sr + i * cin), use_si ? f(d_si + i * cin) : nullptr, f(d_dr + i * cout),
+                      use_di ? f(d_di + i * cout) : nullptr, P->stream);
     if (rc) return rc;
     cudaEventRecord(P->ev[2 * i + 1], P->stream);
     cudaStreamWaitEvent(P->copy_out, P->ev[2 * i + 1], 0);
-    cudaMemcpyAsync(dr + i * cout, d_dr + i * cout, cout * sizeof(float), cudaMemcpyDefault, P->copy_out);
-    if (use_di) cudaMemcpyAsync(di + i * cout, d_di + i * cout, cout * sizeof(float), cudaMemcpyDefault, P->copy_out);
+    cudaMemcpyAsync(h_dr + i * cout, d_dr + i * cout, cout, cudaMemcpyDefault, P->copy_out);
+    if (use_di) cudaMemcpyAsync(h_di + i * cout, d_di + i * cout, cout, cudaMemcpyDefault, P->copy_out);
   }
   cudaError_t e = cudaStreamSynchronize(P->copy_out);
   if (e == cudaSuccess) e = cudaStreamSynchronize(P->stream);
@@ -411,6 +423,10 @@ static int transform_sync(void* plan, const float* sr, const float* si, float* d
   }
   return check_tc_error(*P);
 }
+
+// double arrays of the afft_64_* calls, as the float pointers the plans bind
+static const float* cfp(const double* p) { return reinterpret_cast<const float*>(p); }
+static float* mfp(double* p) { return reinterpret_cast<float*>(p); }
 
 }  // namespace agb
 
@@ -465,31 +481,45 @@ void afft_32_ri_transform(afft_32_ri_type* st, const float* sr, const float* si,
 // ---- fft.h:46 / common.hpp:173-176 ------------------------------------------
 size_t afft_32_align_size(size_t sz) { return (sz + 15) & ~(size_t)15; }
 
-// ---- fft.h:48-80: FP64 is not implemented here ------------------------------
-size_t afft_64_c_memsize(size_t, const size_t*, int, int) {
-  set_error(AFFT_GB300_EINVAL, "FP64 transforms are not implemented");
-  return 0;
+// ---- fft.h:48-80: the same transforms on doubles (FP64 kernels) --------------
+size_t afft_64_c_memsize(size_t ndim, const size_t* dim, int format, int impl) {
+  return memsize_impl(K_C, ndim, dim, 1, format, impl, FORM_F64);
 }
-afft_64_c_type* afft_64_c_create(size_t, const size_t*, int, void*, int) { return nullptr; }
-void afft_64_c_transform(afft_64_c_type*, const double*, const double*, double*, double*) {}
-size_t afft_64_ci_memsize(size_t, const size_t*, int, int) {
-  set_error(AFFT_GB300_EINVAL, "FP64 transforms are not implemented");
-  return 0;
+afft_64_c_type* afft_64_c_create(size_t ndim, const size_t* dim, int format, void* mem, int impl) {
+  return (afft_64_c_type*)create_impl(K_C, ndim, dim, 1, format, mem, impl, FORM_F64);
 }
-afft_64_ci_type* afft_64_ci_create(size_t, const size_t*, int, void*, int) { return nullptr; }
-void afft_64_ci_transform(afft_64_ci_type*, const double*, const double*, double*, double*) {}
-size_t afft_64_r_memsize(size_t, const size_t*, int, int) {
-  set_error(AFFT_GB300_EINVAL, "FP64 transforms are not implemented");
-  return 0;
+void afft_64_c_transform(afft_64_c_type* st, const double* sr, const double* si, double* dr, double* di) {
+  transform_sync(st, cfp(sr), cfp(si), mfp(dr), mfp(di), true);
 }
-afft_64_r_type* afft_64_r_create(size_t, const size_t*, int, void*, int) { return nullptr; }
-void afft_64_r_transform(afft_64_r_type*, const double*, double*, double*) {}
-size_t afft_64_ri_memsize(size_t, const size_t*, int, int) {
-  set_error(AFFT_GB300_EINVAL, "FP64 transforms are not implemented");
-  return 0;
+size_t afft_64_ci_memsize(size_t ndim, const size_t* dim, int format, int impl) {
+  return memsize_impl(K_CI, ndim, dim, 1, format, impl, FORM_F64);
 }
-afft_64_ri_type* afft_64_ri_create(size_t, const size_t*, int, void*, int) { return nullptr; }
-void afft_64_ri_transform(afft_64_ri_type*, const double*, const double*, double*) {}
+afft_64_ci_type* afft_64_ci_create(size_t ndim, const size_t* dim, int format, void* mem, int impl) {
+  return (afft_64_ci_type*)create_impl(K_CI, ndim, dim, 1, format, mem, impl, FORM_F64);
+}
+void afft_64_ci_transform(afft_64_ci_type* st, const double* sr, const double* si, double* dr, double* di) {
+  transform_sync(st, cfp(sr), cfp(si), mfp(dr), mfp(di), true);
+}
+size_t afft_64_r_memsize(size_t ndim, const size_t* dim, int format, int impl) {
+  return memsize_impl(K_R, ndim, dim, 1, format, impl, FORM_F64);
+}
+afft_64_r_type* afft_64_r_create(size_t ndim, const size_t* dim, int format, void* mem, int impl) {
+  return (afft_64_r_type*)create_impl(K_R, ndim, dim, 1, format, mem, impl, FORM_F64);
+}
+void afft_64_r_transform(afft_64_r_type* st, const double* src, double* dr, double* di) {
+  transform_sync(st, cfp(src), nullptr, mfp(dr), mfp(di), true);
+}
+size_t afft_64_ri_memsize(size_t ndim, const size_t* dim, int format, int impl) {
+  return memsize_impl(K_RI, ndim, dim, 1, format, impl, FORM_F64);
+}
+afft_64_ri_type* afft_64_ri_create(size_t ndim, const size_t* dim, int format, void* mem, int impl) {
+  return (afft_64_ri_type*)create_impl(K_RI, ndim, dim, 1, format, mem, impl, FORM_F64);
+}
+void afft_64_ri_transform(afft_64_ri_type* st, const double* sr, const double* si, double* dst) {
+  transform_sync(st, cfp(sr), cfp(si), mfp(dst), nullptr, true);
+}
+
+// ---- fft.h:80 / common.hpp:173-176: 64 bytes of doubles = 8 elements --------
 size_t afft_64_align_size(size_t sz) { return (sz + 7) & ~(size_t)7; }
 
 // ---- fft.h:82-84 ------------------------------------------------------------
@@ -504,20 +534,29 @@ const size_t afft_alignment = 64;
 int afft_gb300_last_error(void) { return g_err; }
 const char* afft_gb300_last_error_string(void) { return g_msg.c_str(); }
 
+// the form flags of a batched or describe call; false when both are set
+static bool split_form(int* format, int* form) {
+  *form = *format & (FORM_TC | FORM_F64);
+  *format &= ~(FORM_TC | FORM_F64);
+  return *form != (FORM_TC | FORM_F64);
+}
+
 size_t afft_gb300_batch_memsize(int kind, size_t ndim, const size_t* dim, size_t batch, int format) {
-  if (kind < 0 || kind > 3) {
-    set_error(AFFT_GB300_EINVAL, "bad kind");
+  int form;
+  if (kind < 0 || kind > 3 || !split_form(&format, &form)) {
+    set_error(AFFT_GB300_EINVAL, "bad kind or form");
     return 0;
   }
-  return memsize_impl(kind, ndim, dim, batch, format & ~FORM_TC, afft_auto, format & FORM_TC);
+  return memsize_impl(kind, ndim, dim, batch, format, afft_auto, form);
 }
 
 void* afft_gb300_batch_create(int kind, size_t ndim, const size_t* dim, size_t batch, int format, void* mem) {
-  if (kind < 0 || kind > 3) {
-    set_error(AFFT_GB300_EINVAL, "bad kind");
+  int form;
+  if (kind < 0 || kind > 3 || !split_form(&format, &form)) {
+    set_error(AFFT_GB300_EINVAL, "bad kind or form");
     return nullptr;
   }
-  return create_impl(kind, ndim, dim, batch, format & ~FORM_TC, mem, afft_auto, format & FORM_TC);
+  return create_impl(kind, ndim, dim, batch, format, mem, afft_auto, form);
 }
 
 int afft_gb300_transform_async(void* plan, const float* sr, const float* si, float* dr, float* di,
@@ -556,9 +595,8 @@ size_t afft_gb300_plan_describe(int kind, size_t ndim, const size_t* dim, size_t
   clear_error();
   int nd;
   long long dims[64];
-  const int form = format & FORM_TC;
-  format &= ~FORM_TC;
-  if (kind < 0 || kind > 3 || ndim > 64 || (ndim && !dim) || batch == 0 ||
+  int form;
+  if (kind < 0 || kind > 3 || !split_form(&format, &form) || ndim > 64 || (ndim && !dim) || batch == 0 ||
       (format != afft_split && format != afft_interleaved) || validate_shape((int)ndim, dim, &nd, dims)) {
     set_error(AFFT_GB300_EINVAL, "bad arguments");
     return 0;

@@ -34,6 +34,13 @@ bool get_rows_c2c_unit(int logl, bool tc, LineKernel* out);
 // rows c2c on interleaved pairs with unit pair strides (float2 accesses)
 bool get_rows_c2c_iunit(int logl, LineKernel* out);
 
+// FP64 kernels (line_fft64.cuh, k_f64_*.cu): rows {C2C, R2C, C2R} up to
+// 2^13 points, cols {C2C (also with the transposing store), R2C, C2R} up to
+// 2^11; `grouped` is null (the multi-transform queue is FP32 only)
+bool get_line_kernel64(int logl, bool cols, int kind, bool tstore, LineKernel* out);
+bool get_rows64(int logl, int kind, LineKernel* out);
+bool get_cols64(int logl, int kind, bool tstore, LineKernel* out);
+
 // split-precision tensor-core form: rows c2c L = 256 or 4096, cols c2c L = 256
 bool get_tc_kernel(int logl, bool cols, bool tstore, LineKernel* out);
 

@@ -138,7 +138,7 @@ extern "C" int afft_gb300_c2c_noalloc(const float* src_re, const float* src_im, 
   long long dims[1] = {(long long)n};
   // the launch list of the ordinary plan, built without touching the device
   auto P = build_plan(inverse ? K_CI : K_C, 1, dims, (long long)batch, afft_split, true);
-  if (!P || P->scratch_floats > 2 * kNoallocMaxElems) {
+  if (!P || P->scratch_elems > 2 * kNoallocMaxElems) {
     set_error(AFFT_GB300_EINVAL, "no-alloc transform: unsupported shape");
     return AFFT_GB300_EINVAL;
   }

@@ -25,6 +25,7 @@
 #include <mutex>
 
 #include "plan.h"
+#include "line_fft64.cuh"
 
 namespace agb {
 
@@ -77,7 +78,7 @@ static float2 root_f(long long m, long long N) {
 
 struct TableCache {
   std::mutex mu;
-  std::map<std::pair<int, long long>, float2*> tables;  // (device * 8 + type, key)
+  std::map<std::pair<int, long long>, void*> tables;  // (device * 8 + type, key)
 };
 static TableCache& tcache() {
   static TableCache* c = new TableCache();  // never destroyed: outlives static plans
@@ -85,22 +86,22 @@ static TableCache& tcache() {
 }
 
 // Device copy of table (type, key) on the current device; `make` builds the
-// host table on the first request only.
+// host table (a std::vector of float2 or double2) on the first request only.
 template <class F>
-static const float2* cached_table(int type, long long key, F make) {
+static auto cached_table(int type, long long key, F make) -> const typename decltype(make())::value_type* {
+  using V = typename decltype(make())::value_type;
   int dev = 0;
   cudaGetDevice(&dev);
   auto& C = tcache();
   std::lock_guard<std::mutex> g(C.mu);
   auto id = std::make_pair(dev * 8 + type, key);
   auto it = C.tables.find(id);
-  if (it != C.tables.end()) return it->second;
-  const std::vector<float2> host = make();
-  float2* d = nullptr;
-  size_t bytes = std::max<size_t>(host.size(), 1) * sizeof(float2);
+  if (it != C.tables.end()) return static_cast<const V*>(it->second);
+  const std::vector<V> host = make();
+  V* d = nullptr;
+  size_t bytes = std::max<size_t>(host.size(), 1) * sizeof(V);
   if (cudaMalloc(&d, bytes) != cudaSuccess) return nullptr;
-  if (!host.empty() &&
-      cudaMemcpy(d, host.data(), host.size() * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess) {
+  if (!host.empty() && cudaMemcpy(d, host.data(), host.size() * sizeof(V), cudaMemcpyHostToDevice) != cudaSuccess) {
     cudaFree(d);
     return nullptr;
   }
@@ -238,6 +239,62 @@ const float2* fourstep_full_table(long long N, long long L2) {
   return cached_table(4, (N << 6) | l2, [&] { return fourstep_full_table_host(N, L2); });
 }
 
+// FP64 tables: the same roots without the rounding to FP32
+static double2 root_d(long long m, long long N) {
+  double c, s;
+  unit_root(m, N, &c, &s);
+  return make_double2(c, s);
+}
+
+template <int LOGL>
+static std::vector<double2> stage_table64() {
+  using S = Sched64<LOGL>;
+  std::vector<double2> t(S::twsize());
+  for (int s = 0; s < S::NSTAGES; s++) {
+    int ns = S::ns(s), R = S::radix(s);
+    if (ns == 1) continue;
+    int off = S::twoff(s);
+    for (int r = 1; r < R; r++)
+      for (int k = 0; k < ns; k++) t[off + (r - 1) * ns + k] = root_d((long long)r * k, (long long)ns * R);
+  }
+  return t;
+}
+
+template <int... Ls>
+static std::vector<double2> stage_table64_dispatch(int logl, std::integer_sequence<int, Ls...>) {
+  std::vector<double2> out;
+  ((logl == Ls ? (void)(out = stage_table64<Ls>()) : (void)0), ...);
+  return out;
+}
+
+std::vector<double2> stage_table64_host(int logl) {
+  return stage_table64_dispatch(logl, std::make_integer_sequence<int, ROWS_MAX_LOG64 + 1>{});
+}
+
+const double2* stage_twiddles64(int logl) {
+  return cached_table(5, logl, [&] { return stage_table64_host(logl); });
+}
+
+const double2* real_twiddles64(long long L) {
+  return cached_table(6, L, [&] {
+    std::vector<double2> t(L);
+    for (long long k = 0; k < L; k++) t[k] = root_d(k, 2 * L);
+    return t;
+  });
+}
+
+const double2* fourstep_full_table64(long long N, long long L2) {
+  int l2 = 0;
+  while ((1LL << l2) < L2) l2++;
+  return cached_table(7, (N << 6) | l2, [&] {
+    const long long L1 = N / L2;
+    std::vector<double2> t(N);
+    for (long long j = 0; j < L2; j++)
+      for (long long k = 0; k < L1; k++) t[j * L1 + k] = root_d(j * k, N);
+    return t;
+  });
+}
+
 // ---------------------------------------------------------------------------
 // plan building
 // ---------------------------------------------------------------------------
@@ -292,7 +349,11 @@ struct Builder {
   long long scr_base = 0;  // floats of scratch reserved below four-step use
   bool dry = false;        // describe only: no device tables
   Tuning tune;             // plan variant
-  explicit Builder(Plan& p, bool d = false) : P(p), dry(d) {}
+  const bool f64;          // FP64 kernels and tables (afft_64_*)
+  explicit Builder(Plan& p, bool d = false) : P(p), dry(d), f64(p.f64()) {}
+
+  // longest line one rows-mode CTA transforms
+  int rows_max() const { return f64 ? ROWS_MAX_LOG64 : ROWS_MAX_LOG; }
 
   // four-step split of an axis of 2^logl points: L1 takes the larger half
   // (measured the better default on GB300 for odd logl), or the smaller one
@@ -304,7 +365,7 @@ struct Builder {
     ok = false;
   }
 
-  void need_scratch(long long floats) { P.scratch_floats = std::max(P.scratch_floats, floats); }
+  void need_scratch(long long elems) { P.scratch_elems = std::max(P.scratch_elems, elems); }
 
   void line(int kind, bool cols, bool tstore, int logl, const IOSpec& in, const IOSpec& out,
             long long nlines, bool inverse, long long tw_n = 0, long long tw_qmask = 0,
@@ -317,11 +378,16 @@ struct Builder {
     Op op;
     op.type = OP_LINE;
     bool tc = P.form == FORM_TC && kind == LK_C2C && get_tc_kernel(logl, cols, tstore, &op.k);
-    const bool unit = !cols && !tstore && kind == LK_C2C && in.es == 1 && out.es == 1;
+    const bool unit = !f64 && !cols && !tstore && kind == LK_C2C && in.es == 1 && out.es == 1;
     // interleaved pairs (im right after re in the same array) with unit pair strides
     auto pairs = [](const IOSpec& v) { return v.es == 2 && v.re.buf == v.im.buf && v.im.off == v.re.off + 1; };
-    const bool iunit = !cols && !tstore && kind == LK_C2C && !tc && pairs(in) && pairs(out);
-    if (unit && get_rows_c2c_unit(logl, tc, &op.k)) {
+    const bool iunit = !f64 && !cols && !tstore && kind == LK_C2C && !tc && pairs(in) && pairs(out);
+    if (f64) {
+      if (!get_line_kernel64(logl, cols, kind, tstore, &op.k)) {
+        fail("no FP64 kernel for this line length");
+        return;
+      }
+    } else if (unit && get_rows_c2c_unit(logl, tc, &op.k)) {
       // same kernel with compile-time element offsets
     } else if (iunit && get_rows_c2c_iunit(logl, &op.k)) {
       // the same on interleaved pairs
@@ -345,12 +411,19 @@ struct Builder {
         fail("kernel shared memory configuration failed");
         return;
       }
-      op.p.tw = stage_twiddles(op.k.stage_logl);
-      if (tw_n) {
-        fourstep_tables(tw_n, &op.p.tw_hi, &op.p.tw_lo, &op.p.tw_lo_bits);
-        op.p.tw_full = fourstep_full_table(tw_n, tw_qmask + 1);
+      if (f64) {
+        // the FP64 kernels read double2 tables through the same fields
+        op.p.tw = reinterpret_cast<const float2*>(stage_twiddles64(op.k.stage_logl));
+        if (tw_n) op.p.tw_full = reinterpret_cast<const float2*>(fourstep_full_table64(tw_n, tw_qmask + 1));
+        if (real_L) op.p.rtw = reinterpret_cast<const float2*>(real_twiddles64(real_L));
+      } else {
+        op.p.tw = stage_twiddles(op.k.stage_logl);
+        if (tw_n) {
+          fourstep_tables(tw_n, &op.p.tw_hi, &op.p.tw_lo, &op.p.tw_lo_bits);
+          op.p.tw_full = fourstep_full_table(tw_n, tw_qmask + 1);
+        }
+        if (real_L) op.p.rtw = real_twiddles(real_L);
       }
-      if (real_L) op.p.rtw = real_twiddles(real_L);
       if (tc) {
         op.p.tc_b = tc_matrix_table();
         op.p.err = tc_error_word();
@@ -363,8 +436,8 @@ struct Builder {
     op.grid = (nlines + op.k.lines_per_cta - 1) / op.k.lines_per_cta * op.k.halves;
     op.threads = op.k.threads;
     op.smem = op.k.smem;
-    if (!dry && (!op.p.tw || (tw_n && (!op.p.tw_hi || !op.p.tw_lo)) ||
-                 (tw_n && tw_n <= kFullTableMax && !op.p.tw_full) || (real_L && !op.p.rtw))) {
+    if (!dry && (!op.p.tw || (tw_n && !f64 && (!op.p.tw_hi || !op.p.tw_lo)) ||
+                 (tw_n && (f64 || tw_n <= kFullTableMax) && !op.p.tw_full) || (real_L && !op.p.rtw))) {
       fail("twiddle table allocation failed");
       return;
     }
@@ -380,7 +453,7 @@ struct Builder {
     op.out = out;
     op.rp.nlines = nlines;
     op.rp.L = L;
-    op.rp.rtw = dry ? nullptr : real_twiddles(L);
+    op.rp.rtw = dry ? nullptr : (f64 ? reinterpret_cast<const float2*>(real_twiddles64(L)) : real_twiddles(L));
     op.rp.inverse = inverse ? 1 : 0;
     op.rp.lines_fastest = lines_fastest ? 1 : 0;
     op.threads = 256;
@@ -432,7 +505,7 @@ struct Builder {
     if (b_bs == 0) b_bs = L * inner;
     int logl = ilog2ll(L);
     if (inner == 1) {
-      if (logl <= ROWS_MAX_LOG) {
+      if (logl <= rows_max()) {
         line(LK_C2C, false, false, logl, io(A, 1, 0, a_bs, 0, 0), io(B, 1, 0, b_bs, 0, 0), outer, inverse);
         return;
       }
@@ -540,7 +613,7 @@ std::unique_ptr<Plan> build_plan(int kind, int ndim, const long long* dims, long
       // a real transform of total size 1 (the reference crashes here):
       // the length-1 DFT, X[0] = x[0] + 0i and x[0] = re X[0]
       b.real1(kind == K_R, batch);
-    } else if (ilog2ll(L) <= ROWS_MAX_LOG) {
+    } else if (ilog2ll(L) <= b.rows_max()) {
       int logl = ilog2ll(L);
       if (kind == K_R)
         b.line(LK_R2C, false, false, logl, io(realv, 1, 0, L, 0, 0), io(dst, 1, 0, L + 1, 0, 0), batch,
@@ -548,6 +621,15 @@ std::unique_ptr<Plan> build_plan(int kind, int ndim, const long long* dims, long
       else
         b.line(LK_C2R, false, false, logl, io(src, 1, 0, L + 1, 0, 0), io(realv, 1, 0, L, 0, 0), batch,
                false, 0, 0, 0, L);
+    } else if (kind == K_R && b.f64) {
+      // FP64: the complex four-step into scratch (its own scratch above),
+      // then the standalone real post-pass into dst
+      View S = split_view(B_SCR, B_SCR, 0);
+      S.im.off = batch * L;
+      b.need_scratch(2 * batch * L);
+      b.scr_base = 2 * batch * L;
+      b.axis(batch, L, 1, realv, S, false, L, L);
+      b.real_pass(io(S, 1, 0, L, 0, 0), io(dst, 1, 0, L + 1, 0, 0), batch, L, false, false);
     } else if (kind == K_R) {
       // four-step pass A (twiddle, transposing store) into scratch, then
       // pass B over mirrored column pairs with the real post-pass fused,
@@ -571,7 +653,7 @@ std::unique_ptr<Plan> build_plan(int kind, int ndim, const long long* dims, long
       // the paired pass A runs over the shorter half by default (the longer
       // one when tuned so, where its kernel exists: pass A lengths <= 512)
       const int l1p = b.tune.split ? (logl + 1) / 2 : logl / 2;
-      if (logl <= 19 && b.tune.real_inv == 0 && l1p <= 9) {
+      if (!b.f64 && logl <= 19 && b.tune.real_inv == 0 && l1p <= 9) {
         // inverse four-step pass A over mirrored column pairs with the real
         // pre-pass fused into its loads (twiddle, transposing store into
         // scratch), then pass B into dst's interleaved view.  Pass A takes
@@ -686,9 +768,9 @@ std::string describe_plan(const Plan& P) {
   std::string o = "{";
   char buf[1024];
   snprintf(buf, sizeof buf,
-           "\"kind\":%d,\"format\":%d,\"batch\":%lld,\"in_elems\":%lld,\"out_elems\":%lld,"
-           "\"scratch_floats\":%lld,\"ops\":[",
-           P.kind, P.format, P.batch, P.in_elems, P.out_elems, P.scratch_floats);
+           "\"kind\":%d,\"format\":%d,\"f64\":%d,\"batch\":%lld,\"in_elems\":%lld,\"out_elems\":%lld,"
+           "\"scratch_elems\":%lld,\"ops\":[",
+           P.kind, P.format, P.f64() ? 1 : 0, P.batch, P.in_elems, P.out_elems, P.scratch_elems);
   o += buf;
   for (size_t i = 0; i < P.ops.size(); i++) {
     const Op& op = P.ops[i];
@@ -730,12 +812,16 @@ Plan::~Plan() {
   for (auto e : ev) cudaEventDestroy(e);
 }
 
-static inline float* resolve(const Ref& r, float* const* base) { return base[r.buf] ? base[r.buf] + r.off : nullptr; }
+// element `off` of buffer `buf`, elements of `esz` bytes (4, or 8 in FP64 plans)
+static inline float* resolve(const Ref& r, float* const* base, size_t esz) {
+  return base[r.buf] ? reinterpret_cast<float*>(reinterpret_cast<char*>(base[r.buf]) + r.off * (long long)esz)
+                     : nullptr;
+}
 
-static LineIO bind(const IOSpec& s, float* const* base) {
+static LineIO bind(const IOSpec& s, float* const* base, size_t esz) {
   LineIO o;
-  o.re = resolve(s.re, base);
-  o.im = resolve(s.im, base);
+  o.re = resolve(s.re, base, esz);
+  o.im = resolve(s.im, base, esz);
   o.es = s.es;
   o.lo = s.lo;
   o.hi = s.hi;
@@ -751,8 +837,8 @@ bool op_tables_ok(const Op& op) {
 }
 
 int Plan::launch(const float* src_re, const float* src_im, float* dst_re, float* dst_im, cudaStream_t st) {
-  if (scratch_floats > 0 && !scratch) {
-    if (cudaMalloc(&scratch, (size_t)scratch_floats * sizeof(float)) != cudaSuccess) {
+  if (scratch_elems > 0 && !scratch) {
+    if (cudaMalloc(&scratch, (size_t)scratch_elems * esize()) != cudaSuccess) {
       cudaGetLastError();
       set_error(3, "scratch allocation failed");
       return 3;
@@ -767,27 +853,32 @@ int Plan::launch(const float* src_re, const float* src_im, float* dst_re, float*
       return 4;
     }
   }
+  const size_t esz = esize();
+  const bool dbl = f64();
   for (auto& op : ops) {
     if (op.type == OP_LINE) {
       LineParams p = op.p;
-      p.in = bind(op.in, base);
-      p.out = bind(op.out, base);
+      p.in = bind(op.in, base, esz);
+      p.out = bind(op.out, base, esz);
       op.k.fn<<<(unsigned)op.grid, op.threads, op.smem, st>>>(p);
     } else if (op.type == OP_REAL) {
       RealPassParams rp = op.rp;
-      rp.in = bind(op.in, base);
-      rp.out = bind(op.out, base);
-      real_pass_kernel<<<(unsigned)op.grid, op.threads, 0, st>>>(rp);
+      rp.in = bind(op.in, base, esz);
+      rp.out = bind(op.out, base, esz);
+      if (dbl) real_pass_kernel64<<<(unsigned)op.grid, op.threads, 0, st>>>(rp);
+      else real_pass_kernel<<<(unsigned)op.grid, op.threads, 0, st>>>(rp);
     } else if (op.type == OP_COPY) {
       CopyParams cp = op.cp;
-      cp.in = bind(op.in, base);
-      cp.out = bind(op.out, base);
-      copy_lines_kernel<<<(unsigned)op.grid, op.threads, 0, st>>>(cp);
+      cp.in = bind(op.in, base, esz);
+      cp.out = bind(op.out, base, esz);
+      if (dbl) copy_lines_kernel64<<<(unsigned)op.grid, op.threads, 0, st>>>(cp);
+      else copy_lines_kernel<<<(unsigned)op.grid, op.threads, 0, st>>>(cp);
     } else {
       RealPassParams rp = op.rp;
-      rp.in = bind(op.in, base);
-      rp.out = bind(op.out, base);
-      real1_kernel<<<(unsigned)op.grid, op.threads, 0, st>>>(rp);
+      rp.in = bind(op.in, base, esz);
+      rp.out = bind(op.out, base, esz);
+      if (dbl) real1_kernel64<<<(unsigned)op.grid, op.threads, 0, st>>>(rp);
+      else real1_kernel<<<(unsigned)op.grid, op.threads, 0, st>>>(rp);
     }
   }
   cudaError_t e = cudaGetLastError();

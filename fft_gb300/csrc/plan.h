@@ -51,14 +51,16 @@ struct Op {
 void set_error(int code, const std::string& msg);
 void clear_error();
 
-// Form flag, OR-ed into the format argument of the batched and describe
-// entry points: split-precision tensor-core butterflies where eligible.
+// Form flags, OR-ed into the format argument of the batched and describe
+// entry points: split-precision tensor-core butterflies where eligible
+// (FORM_TC), or FP64 data and arithmetic (FORM_F64, the afft_64_* path).
 constexpr int FORM_TC = 0x100;
+constexpr int FORM_F64 = 0x200;
 
 struct Plan {
   int kind = K_C;
   int format = 0;              // afft_split / afft_interleaved
-  int form = 0;                // 0 plain FP32, FORM_TC split-precision tensor cores
+  int form = 0;                // 0 plain FP32, FORM_TC split-precision tensor cores, FORM_F64 FP64
   int ndim = 1;
   long long dims[64] = {0};
   long long batch = 1;
@@ -66,7 +68,7 @@ struct Plan {
   long long out_elems = 0;
   int device = 0;
   std::vector<Op> ops;
-  long long scratch_floats = 0;
+  long long scratch_elems = 0;   // scratch elements (floats, doubles in FP64 plans)
   long long real_L_of_op = 0;
   float* scratch = nullptr;
   cudaStream_t stream = nullptr;
@@ -82,6 +84,8 @@ struct Plan {
   std::mutex mu;
 
   ~Plan();
+  bool f64() const { return (form & FORM_F64) != 0; }
+  size_t esize() const { return f64() ? sizeof(double) : sizeof(float); }   // bytes per element
   // Launch all ops on `stream`; pointers must be device-accessible.
   int launch(const float* src_re, const float* src_im, float* dst_re, float* dst_im,
              cudaStream_t stream);
@@ -127,6 +131,13 @@ void fourstep_tables(long long N, const float2** hi, const float2** lo, int* lo_
 // N <= kFullTableMax (nullptr above): one coalesced load per element.
 constexpr long long kFullTableMax = 1LL << 20;
 const float2* fourstep_full_table(long long N, long long L2);
+// FP64 tables (computed in FP64, no rounding): stage twiddles of the FP64
+// line kernels, W_{2L}^k (k < L), and the four-step matrix W_N^{t2 k} at
+// [t2 * L1 + k] for any N
+const double2* stage_twiddles64(int logl);
+const double2* real_twiddles64(long long L);
+const double2* fourstep_full_table64(long long N, long long L2);
+std::vector<double2> stage_table64_host(int logl);
 std::vector<float2> fourstep_full_table_host(long long N, long long L2);
 // The same tables on the host, without touching the device.
 std::vector<float2> stage_table_host(int logl);

@@ -104,7 +104,7 @@ static int build_queue(QueueImpl& Q) {
     }
     plan_of.push_back(it->second);
     scr_off.push_back(arena_floats);
-    arena_floats += (it->second->scratch_floats + 63) / 64 * 64;
+    arena_floats += (it->second->scratch_elems + 63) / 64 * 64;
   }
   if (arena_floats && cudaMalloc(&Q.arena, (size_t)arena_floats * sizeof(float)) != cudaSuccess) {
     cudaGetLastError();
@@ -301,6 +301,10 @@ afft_gb300_queue* afft_gb300_queue_create_ex(const afft_gb300_desc* descs, size_
   clear_error();
   if (!descs && count) {
     set_error(AFFT_GB300_EINVAL, "null descriptor array");
+    return nullptr;
+  }
+  if (flags & ~FORM_TC) {   // FP32 data only (FP64 transforms have no grouped kernels)
+    set_error(AFFT_GB300_EINVAL, "queue flags: 0 or AFFT_GB300_FORM_TC");
     return nullptr;
   }
   auto* q = new afft_gb300_queue();

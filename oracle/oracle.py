@@ -192,48 +192,50 @@ def ref_lib():
         L = ctypes.CDLL(REF_PATH)
         P = ctypes.c_void_p
         S = ctypes.c_size_t
-        for k in ("c", "ci", "r", "ri"):
-            ms = getattr(L, "afft_32_%s_memsize" % k)
-            ms.restype = S
-            ms.argtypes = [S, P, ctypes.c_int, ctypes.c_int]
-            cr = getattr(L, "afft_32_%s_create" % k)
-            cr.restype = P
-            cr.argtypes = [S, P, ctypes.c_int, P, ctypes.c_int]
-            getattr(L, "afft_32_%s_transform" % k).restype = None
-        L.afft_32_c_transform.argtypes = [P, P, P, P, P]
-        L.afft_32_ci_transform.argtypes = [P, P, P, P, P]
-        L.afft_32_r_transform.argtypes = [P, P, P, P]
-        L.afft_32_ri_transform.argtypes = [P, P, P, P]
+        for bits in ("32", "64"):
+            for k in ("c", "ci", "r", "ri"):
+                ms = getattr(L, "afft_%s_%s_memsize" % (bits, k))
+                ms.restype = S
+                ms.argtypes = [S, P, ctypes.c_int, ctypes.c_int]
+                cr = getattr(L, "afft_%s_%s_create" % (bits, k))
+                cr.restype = P
+                cr.argtypes = [S, P, ctypes.c_int, P, ctypes.c_int]
+                tr = getattr(L, "afft_%s_%s_transform" % (bits, k))
+                tr.restype = None
+                tr.argtypes = [P, P, P, P, P] if k in ("c", "ci") else [P, P, P, P]
         L.afft_supported.argtypes = [ctypes.c_int]
         _ref = L
     return _ref
 
 
-def ref_run(kind, dims, a, b=None, impl=0):
-    """One transform through the reference library's own C API (fft.h)."""
+def ref_run(kind, dims, a, b=None, impl=0, bits=32):
+    """One transform through the reference library's own C API (fft.h):
+    afft_32_* on float arrays, or afft_64_* on double arrays (bits=64)."""
     L = ref_lib()
+    dt = np.float32 if bits == 32 else np.float64
+    fn = lambda what: getattr(L, "afft_%d_%s_%s" % (bits, kind, what))
     d = np.array(dims, dtype=np.uint64)
-    ms = getattr(L, "afft_32_%s_memsize" % kind)(len(d), _p(d), 0, impl)
+    ms = fn("memsize")(len(d), _p(d), 0, impl)
     if ms == 0:
         raise ValueError("reference rejected %r impl=%d" % (dims, impl))
     mem = np.zeros(ms + 64, np.uint8)
-    st = getattr(L, "afft_32_%s_create" % kind)(len(d), _p(d), 0, _p(mem), impl)
+    st = fn("create")(len(d), _p(d), 0, _p(mem), impl)
     n = int(np.prod(dims, dtype=np.int64))
     h = half_elems(dims)
-    a = np.ascontiguousarray(a, np.float32).ravel()
-    b = None if b is None else np.ascontiguousarray(b, np.float32).ravel()
+    a = np.ascontiguousarray(a, dt).ravel()
+    b = None if b is None else np.ascontiguousarray(b, dt).ravel()
     if kind in ("c", "ci"):
-        ore = np.zeros(n, np.float32)
-        oim = np.zeros(n, np.float32)
-        getattr(L, "afft_32_%s_transform" % kind)(ctypes.c_void_p(st), _p(a), _p(b), _p(ore), _p(oim))
+        ore = np.zeros(n, dt)
+        oim = np.zeros(n, dt)
+        fn("transform")(ctypes.c_void_p(st), _p(a), _p(b), _p(ore), _p(oim))
         return ore, oim
     if kind == "r":
-        ore = np.zeros(h, np.float32)
-        oim = np.zeros(h, np.float32)
-        L.afft_32_r_transform(ctypes.c_void_p(st), _p(a), _p(ore), _p(oim))
+        ore = np.zeros(h, dt)
+        oim = np.zeros(h, dt)
+        fn("transform")(ctypes.c_void_p(st), _p(a), _p(ore), _p(oim))
         return ore, oim
-    out = np.zeros(n, np.float32)
-    L.afft_32_ri_transform(ctypes.c_void_p(st), _p(a), _p(b), _p(out))
+    out = np.zeros(n, dt)
+    fn("transform")(ctypes.c_void_p(st), _p(a), _p(b), _p(out))
     return out
 
 

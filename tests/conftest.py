@@ -29,3 +29,16 @@ def golden():
     z = np.load(os.path.join(here, "afft_golden.npz"))
     idx = json.load(open(os.path.join(here, "afft_golden.json")))
     return z, idx["cases"]
+
+
+@pytest.fixture(scope="session")
+def golden64():
+    """The reference afft library's own double outputs (afft_64_*, scalar
+    backend; tests/golden/make_golden.py --f64).  Inputs are float32 values
+    to be widened to double."""
+    import json
+    import numpy as np
+    here = os.path.join(ROOT, "tests", "golden")
+    z = np.load(os.path.join(here, "afft_golden64.npz"))
+    idx = json.load(open(os.path.join(here, "afft_golden64.json")))
+    return z, idx["cases"]

@@ -15,7 +15,14 @@ afft computes, including how it ignores the imaginary parts of planes 0 and
 d0/2.  Case 'c1' is the reference harness's own n=1024 input (default seed,
 re block then im block).
 
-    python tests/golden/make_golden.py
+With ``--f64`` it writes ``afft_golden64.npz`` / ``.json`` instead: the same
+cases plus the lengths where FP64 plans change shape, through the
+reference's double entry points (afft_64_*, fft.h:52-80).  Inputs are the
+same mt19937 floats (stored as float32, exact) widened to double; the output
+stored is afft_scalar's, and the json records how far afft_auto's differs.
+
+    python tests/golden/make_golden.py          # FP32 fixtures
+    python tests/golden/make_golden.py --f64    # FP64 fixtures
 """
 import json
 import os
@@ -42,11 +49,14 @@ SHAPES = [
     [1, 64], [16, 1, 8], [32, 1], [1, 1, 1], [1, 1, 4, 1],
 ]
 KINDS = ["c", "ci", "r", "ri"]
+# FP64 fixtures also cover the lengths where the FP64 plans change shape
+# (one CTA up to 2^13 points in rows, 2^11 in cols)
+SHAPES64 = SHAPES + [[16384], [32768], [4096, 4]]
 
 
-def cases():
+def cases(shapes=SHAPES):
     seed = 1
-    for dims in SHAPES:
+    for dims in shapes:
         n = int(np.prod(dims))
         for kind in KINDS:
             # the reference crashes on real transforms of total size 1
@@ -56,8 +66,49 @@ def cases():
             yield "%s_%s" % (kind, "x".join(map(str, dims))), kind, dims, seed
 
 
+def main_f64():
+    arrays = {}
+    index = []
+    for name, kind, dims, seed in cases(SHAPES64):
+        # the longer real shapes only for the real kinds (their complex
+        # cases repeat the four-step of [16384]), keeping the fixture small
+        if dims in ([32768], [4096, 4]) and kind in ("c", "ci"):
+            continue
+        n = int(np.prod(dims))
+        h = O.half_elems(dims)
+        m = 2 * n if kind in ("c", "ci") else (n if kind == "r" else 2 * h)
+        v32 = O.mt19937_uniform(m, seed)
+        v = v32.astype(np.float64)
+        if kind in ("c", "ci"):
+            a, b = v[:n], v[n:]
+            arrays[name + "/in0"], arrays[name + "/in1"] = v32[:n], v32[n:]
+        elif kind == "r":
+            a, b = v, None
+            arrays[name + "/in0"] = v32
+        else:
+            a, b = v[:h], v[h:]
+            arrays[name + "/in0"], arrays[name + "/in1"] = v32[:h], v32[h:]
+        out = O.ref_run(kind, dims, a, b, AFFT_SCALAR, bits=64)
+        alt = O.ref_run(kind, dims, a, b, AFFT_AUTO, bits=64)
+        if kind == "ri":
+            arrays[name + "/scalar0"] = out
+        else:
+            arrays[name + "/scalar0"], arrays[name + "/scalar1"] = out
+        index.append({"name": name, "kind": kind, "dims": dims, "seed": seed,
+                      "auto_vs_scalar_rel_l2": O.rel_l2(alt, out)})
+    np.savez_compressed(os.path.join(HERE, "afft_golden64.npz"), **arrays)
+    with open(os.path.join(HERE, "afft_golden64.json"), "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py --f64",
+                   "reference_impls": {"scalar": AFFT_SCALAR},
+                   "inputs": "float32 values, widened to double for the transform",
+                   "cases": index}, f, indent=1)
+    print("wrote %d FP64 cases" % len(index))
+
+
 def main():
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "all", "ref"], check=True)
+    if "--f64" in sys.argv[1:]:
+        return main_f64()
     arrays = {}
     index = []
     for name, kind, dims, seed in cases():

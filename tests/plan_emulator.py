@@ -259,7 +259,7 @@ def buffer_sizes(desc):
     src_im = ie if (cin and not inter) else None
     dst_re = oe * (2 if (inter and cout) else 1)
     dst_im = oe if (cout and not inter) else None
-    return [src_re, src_im, dst_re, dst_im, desc["scratch_floats"] or None]
+    return [src_re, src_im, dst_re, dst_im, desc["scratch_elems"] or None]
 
 
 def run(desc, a, b=None):

@@ -77,9 +77,12 @@ def test_rejections_before_device(kind):
     assert _memsize(kind, [16], impl=G.afft_avx2) == 0
     # unknown format: (size_t)-1 as afft's impl.hpp:38-39
     assert _memsize(kind, [16], fmt=7) == ctypes.c_size_t(-1).value
-    # FP64: unsupported convention
-    arr = (ctypes.c_size_t * 1)(16)
-    assert getattr(G.lib(), "afft_64_%s_memsize" % kind)(1, arr, 0, 0) == 0
+    # FP64 entry points: the same validation
+    ms64 = getattr(G.lib(), "afft_64_%s_memsize" % kind)
+    assert ms64(1, (ctypes.c_size_t * 1)(12), 0, 0) == 0
+    assert G.last_error()[0] == 1
+    assert ms64(1, (ctypes.c_size_t * 1)(16), 0, G.afft_avx2) == 0
+    assert ms64(1, (ctypes.c_size_t * 1)(16), 7, 0) == ctypes.c_size_t(-1).value
 
 
 @pytest.mark.skipif(cuda_available(), reason="checks the no-device path")

@@ -110,3 +110,20 @@ def test_port32_batch_threads():
     assert np.array_equal(r1[0], r4[0]) and np.array_equal(r1[1], r4[1])
     one = p(a[256:512], b[256:512])
     assert np.array_equal(one[0], r1[0][256:512])
+
+
+def test_oracle64_against_reference_fp64_outputs(golden64):
+    # the FP64 oracle against the reference's own double transforms
+    # (afft_64_*): both FP64, so they agree to a few units of roundoff
+    z, cases = golden64
+    worst = 0.0
+    for case in cases:
+        nm, kind, dims = case["name"], case["kind"], case["dims"]
+        a = z[nm + "/in0"].astype(np.float64)
+        b = z[nm + "/in1"].astype(np.float64) if nm + "/in1" in z else None
+        ref = z[nm + "/scalar0"] if kind == "ri" else (z[nm + "/scalar0"], z[nm + "/scalar1"])
+        err = O.rel_l2(O.oracle64(kind, dims, a, b), ref)
+        worst = max(worst, err)
+        assert err <= 1e-14, (nm, err)
+        assert case["auto_vs_scalar_rel_l2"] <= 1e-14, nm
+    print("worst oracle64 vs afft_64 rel-L2: %.2e" % worst)

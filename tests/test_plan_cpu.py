@@ -65,3 +65,41 @@ def test_launch_counts():
     assert len(describe("r", [1 << 20], 2)["ops"]) == 2
     assert len(describe("ri", [1 << 20], 2)["ops"]) == 2
     assert len(describe("ri", [1 << 22], 1)["ops"]) == 3
+
+
+# FP64 plans (afft_64_*): rows up to 2^13 points, cols up to 2^11, standalone
+# real passes beyond one CTA; the same emulation and oracle bar
+SHAPES64 = [[1], [2], [8], [16], [512], [8192], [16384], [32768], [1 << 17], [1 << 22],
+            [2, 2], [4096, 4], [8, 4096], [2048, 2], [16, 2048, 2], [2, 16384], [2, 4, 8], [4, 1, 1, 8]]
+
+
+@pytest.mark.parametrize("dims", SHAPES64, ids=lambda d: "x".join(map(str, d)))
+@pytest.mark.parametrize("kind", ["c", "ci", "r", "ri"])
+def test_plan_emulation_f64(kind, dims):
+    n = int(np.prod(dims))
+    for fmt in (G.afft_split, G.afft_interleaved):
+        for batch in (1, 3):
+            if n * batch > (1 << 20) and batch > 1:
+                continue
+            desc = describe(kind, dims, batch, fmt | G.FORM_F64)
+            assert desc["f64"] == 1
+            for op in desc["ops"]:
+                if op["type"] == "line":
+                    assert op["lk"] in (0, 1, 2) and op["halves"] == 1 and op["tc"] == 0, op
+            a, b = _inputs(kind, dims, batch, n + batch)
+            got = run(desc, a, b)
+            ref = _expected(kind, dims, batch, a, b)
+            assert O.rel_l2(got, ref) < 1e-12, (kind, dims, batch, fmt)
+
+
+def test_launch_counts_f64():
+    F = G.FORM_F64
+    assert len(describe("c", [8192], 4, F)["ops"]) == 1
+    assert len(describe("c", [16384], 4, F)["ops"]) == 2
+    assert len(describe("r", [16384], 4, F)["ops"]) == 1          # 8192 complex points, one CTA
+    assert len(describe("r", [32768], 4, F)["ops"]) == 3          # four-step + standalone post-pass
+    assert len(describe("ri", [32768], 4, F)["ops"]) == 3         # standalone pre-pass + four-step
+    d = describe("r", [4096, 4096], 1, F)
+    assert len(d["ops"]) == 2 and d["ops"][0]["logl"] == 11 and d["ops"][0]["C"] == 4
+    assert describe("c", [256, 256, 256], 1, F)["scratch_elems"] == 0
+    assert len(describe("c", [1 << 22], 1, F)["ops"]) == 2
