@@ -6,7 +6,11 @@ per array pair), inputs i.i.d. standard normal from a seed; one step = the
 forward transform of the batch followed by the inverse transform.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--config c2|c1|c3a|c3b|c3c|c4|c5]
+                    [--config c2|c1|c3a|c3b|c3c|c4|c5] [--form plain|tc|f64]
+
+--form f64 runs the same configs on double data through the FP64 kernels
+(afft_64_*); its roofline is the FP64 pipe (nominal GB300 FP64 rate), its CPU
+baseline the oracle's FP64 port of afft.
 
 value      GFLOP/s by afft's convention (5 N log2 N complex, 2.5 N log2 N
            real, testing.cpp:1027), inputs resident in HBM, CUDA events on
@@ -56,7 +60,11 @@ CONFIGS = {
 
 
 FORMS = {"plain": "plain FP32 Stockham",
-         "tc": "split-precision tensor cores (tcgen05 DFT-16, FP16 hi+lo, FP32 accumulate) where eligible"}
+         "tc": "split-precision tensor cores (tcgen05 DFT-16, FP16 hi+lo, FP32 accumulate) where eligible",
+         "f64": "FP64 data and arithmetic (afft_64_*): radix-8 Stockham FP64 kernels"}
+
+# GB300's nominal FP64 rate (GFLOP/s); MEASURED_PEAKS.json has no FP64 figure
+FP64_NOMINAL_GFLOPS = 1250.0
 
 
 def peaks():
@@ -85,14 +93,15 @@ def flops_of(kind, dims, batch):
     return c * n * math.log2(n) * batch if n > 1 else 0.0
 
 
-def bytes_of(kind, dims, batch):
-    """Algorithmic bytes of one transform pass: one read + one write."""
+def bytes_of(kind, dims, batch, esize=4):
+    """Algorithmic bytes of one transform pass: one read + one write
+    (esize bytes per real value: 4 for FP32, 8 for FP64)."""
     n = int(np.prod(dims))
     d = [x for x in dims if x != 1] or [1]
     h = (d[0] // 2 + 1) * (n // d[0])
     if kind in ("c", "ci"):
-        return 16 * n * batch
-    return (4 * n + 8 * h) * batch
+        return 4 * esize * n * batch
+    return (esize * n + 2 * esize * h) * batch
 
 
 class ClockSampler:
@@ -193,38 +202,43 @@ def accuracy(kind, dims, batch, src, mid, back, with_inv):
     return out
 
 
-def make_inputs(kind, dims, batch, seed, dev):
+def make_inputs(kind, dims, batch, seed, dev, dtype=None):
     import torch
+    dtype = dtype or torch.float32
     n = int(np.prod(dims))
     d = [x for x in dims if x != 1] or [1]
     h = (d[0] // 2 + 1) * (n // d[0])
     g = torch.Generator(device=dev)
     g.manual_seed(seed)
     m = n * batch
+    E = lambda k: torch.empty(k, device=dev, dtype=dtype)
     if kind == "c":
-        a = torch.randn(m, generator=g, device=dev)
-        b = torch.randn(m, generator=g, device=dev)
-        return (a, b), (torch.empty(m, device=dev), torch.empty(m, device=dev)), \
-               (torch.empty(m, device=dev), torch.empty(m, device=dev))
+        a = torch.randn(m, generator=g, device=dev, dtype=dtype)
+        b = torch.randn(m, generator=g, device=dev, dtype=dtype)
+        return (a, b), (E(m), E(m)), (E(m), E(m))
     # real: x -> half spectrum -> x
-    a = torch.randn(m, generator=g, device=dev)
-    return (a,), (torch.empty(h * batch, device=dev), torch.empty(h * batch, device=dev)), \
-           (torch.empty(m, device=dev),)
+    a = torch.randn(m, generator=g, device=dev, dtype=dtype)
+    return (a,), (E(h * batch), E(h * batch)), (E(m),)
 
 
-def cpu_port_rate(kind, dims, batch_total, threads, budget_s):
-    """GFLOP/s of the oracle's FP32 port of afft on `threads` host threads, on
-    a bounded sample of the workload (forward + inverse per transform)."""
+def cpu_port_rate(kind, dims, batch_total, threads, budget_s, f64=False):
+    """GFLOP/s of the oracle's FP32 (or FP64) port of afft on `threads` host
+    threads, on a bounded sample of the workload (forward + inverse per
+    transform)."""
     from oracle import oracle as O
     n = int(np.prod(dims))
-    fwd = O.Port32(kind, dims)
-    inv = O.Port32("ci" if kind == "c" else "ri", dims)
+    Port = O.Port64 if f64 else O.Port32
+    vt = np.float64 if f64 else np.float32
+    fwd = Port(kind, dims)
+    inv = Port("ci" if kind == "c" else "ri", dims)
     rng = np.random.default_rng(0)
     # sample size: grow until a pass takes >= budget/4, capped by the workload
-    sample = max(threads, 1)
+    # (a single transform runs on one thread, as afft's own calls do)
+    sample = max(1, min(threads, batch_total))
+    threads = min(threads, sample)
     while True:
-        a = rng.standard_normal(fwd.in_elems * sample).astype(np.float32)
-        b = None if kind == "r" else rng.standard_normal(fwd.in_elems * sample).astype(np.float32)
+        a = rng.standard_normal(fwd.in_elems * sample).astype(vt)
+        b = None if kind == "r" else rng.standard_normal(fwd.in_elems * sample).astype(vt)
         t0 = time.perf_counter()
         out = fwd(a, b, batch=sample, threads=threads)
         if kind == "c":
@@ -243,7 +257,8 @@ def cpu_port_rate(kind, dims, batch_total, threads, budget_s):
         inv(out[0], out[1], batch=sample, threads=threads)
     dt = time.perf_counter() - t0
     fl = 2 * flops_of(kind, dims, sample) * reps
-    return fl / dt / 1e9, "%d of %d transforms (fwd+inv) x %d reps, %.1f s" % (sample, batch_total, reps, dt)
+    return fl / dt / 1e9, "%d of %d transforms (fwd+inv) x %d reps, %.1f s" % (sample, batch_total, reps, dt), \
+        threads
 
 
 def run_reference(args, cfg):
@@ -257,17 +272,18 @@ def run_reference(args, cfg):
     # bounded: each step is a sample of the workload sized to ~1-3 s
     rates = []
     sample_desc = ""
+    f64 = args.form == "f64"
     for i in range(args.warmup + args.steps):
-        r, sample_desc = cpu_port_rate(kind, dims, batch, threads, budget_s=1.5)
+        r, sample_desc, threads_used = cpu_port_rate(kind, dims, batch, threads, budget_s=1.5, f64=f64)
         if i >= args.warmup:
             rates.append(r)
     value = statistics.median(rates)
     line = {"metric": "GFLOP/s (5N·log2N) & HBM GB/s: TC-split+batched vs plain FP32 at rel-L2≤5e-6",
             "value": round(value, 3), "unit": "GFLOP/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32", "data": "synthetic (seeded standard normal)", "impl": "reference",
-            "config": {"workload": desc},
-            "cpu_baseline": {"value": round(value, 3), "unit": "GFLOP/s", "cores": threads, "kind": "port",
+            "dtype": "f64" if f64 else "f32", "data": "synthetic (seeded standard normal)", "impl": "reference",
+            "config": {"workload": desc, "form": "FP64 port of afft" if f64 else "FP32 port of afft"},
+            "cpu_baseline": {"value": round(value, 3), "unit": "GFLOP/s", "cores": threads_used, "kind": "port",
                              "sample": sample_desc},
             "e2e": {"value": round(value, 3), "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -376,9 +392,12 @@ def run_ours(args, cfg):
         batch = args.batch
         desc = desc + " (batch overridden to %d)" % batch
     form = None if args.form == "plain" else args.form
+    f64 = args.form == "f64"
+    dtype = torch.float64 if f64 else torch.float32
+    esize = 8 if f64 else 4
     fwd = G.BatchPlan(kind, dims, batch, form=form)
     inv = G.BatchPlan("ci" if kind == "c" else "ri", dims, batch, form=form) if with_inv else None
-    src, mid, back = make_inputs(kind, dims, batch, rank_seed(rank), dev)
+    src, mid, back = make_inputs(kind, dims, batch, rank_seed(rank), dev, dtype)
     stream = torch.cuda.Stream(device=dev)   # our kernels and the events share it
     torch.cuda.synchronize()
 
@@ -452,41 +471,56 @@ def run_ours(args, cfg):
     # end to end through the C ABI with pinned host buffers
     e2e = None
     if not args.no_e2e:
-        e2e = e2e_rate(args, kind, dims, batch, src, G, torch, world)
+        e2e = e2e_rate(args, kind, dims, batch, src, G, torch, world, form=form, dtype=dtype)
 
     if rank != 0:
         if world > 1:
             torch.distributed.destroy_process_group()
         return
     hbm, peak_src = peaks()
-    alg_bytes = bytes_of(kind, dims, batch)
+    alg_bytes = bytes_of(kind, dims, batch, esize)
     achieved = alg_bytes / (fwd_ms / 1e3) / 1e9
     # the same time against what the plan's passes must move between them
     # (each launch reads its input and writes its output once)
-    pb = G.pass_bytes(G.describe(kind, dims, batch))
+    pb = G.pass_bytes(G.describe(kind, dims, batch, G.FORM_F64 if f64 else 0)) * esize // 4
     passes = {"launches": fwd.launches, "bytes": pb, "achieved": round(pb / (fwd_ms / 1e3) / 1e9, 1),
               "frac": round(pb / (fwd_ms / 1e3) / 1e9 / hbm, 4), "unit": "GB/s"}
     cpu = None
     if not args.no_cpu:
         threads = os.cpu_count() or 1
-        rate, sample = cpu_port_rate(kind, dims, batch, threads, budget_s=args.cpu_budget)
-        cpu = {"value": round(rate, 3), "unit": "GFLOP/s", "cores": threads, "kind": "port", "sample": sample}
+        rate, sample, used = cpu_port_rate(kind, dims, batch, threads, budget_s=args.cpu_budget, f64=f64)
+        cpu = {"value": round(rate, 3), "unit": "GFLOP/s", "cores": used, "kind": "port", "sample": sample}
+    if f64:
+        # FP64 arithmetic, not HBM, bounds the FP64 kernels on GB300
+        fwd_gflops = flops_of(kind, dims, batch) / (fwd_ms / 1e3) / 1e9
+        roofline = {"bound": "fp64", "achieved": round(fwd_gflops, 1), "peak": FP64_NOMINAL_GFLOPS,
+                    "unit": "GFLOP/s", "frac": round(fwd_gflops / FP64_NOMINAL_GFLOPS, 4), "traffic": None,
+                    "peak_source": "nominal (no measured FP64 figure)",
+                    "kernel": "forward plan (%d launch%s), %.4f ms per launch" % (
+                        fwd.launches, "es" if fwd.launches > 1 else "", fwd_ms / fwd.launches),
+                    "hbm": {"achieved": round(achieved, 1), "peak": hbm, "frac": round(achieved / hbm, 4),
+                            "unit": "GB/s"},
+                    "passes": passes}
+    else:
+        roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                    "frac": round(achieved / hbm, 4),
+                    "traffic": args.traffic if args.traffic else (measured_traffic(cfg) if not args.batch and args.form == "plain" else None),
+                    "peak_source": peak_src,
+                    "kernel": "forward plan (%d launch%s), %.4f ms per launch" % (
+                        fwd.launches, "es" if fwd.launches > 1 else "", fwd_ms / fwd.launches),
+                    "passes": passes}
     line = {
         "metric": "GFLOP/s (5N·log2N) & HBM GB/s: TC-split+batched vs plain FP32 at rel-L2≤5e-6",
         "value": round(value, 2), "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": round(ms_step, 4), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded standard normal)",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if f64 else "f32",
+        "data": "synthetic (seeded standard normal)",
         "config": {"workload": desc, "kind": kind, "dims": dims, "batch_per_gpu": batch,
-                   "form": FORMS[args.form], "l2": "inputs larger than L2 (512 MiB per array pair)"
-                   if bytes_of(kind, dims, batch) > 2 * 129e6 else "working set may fit L2",
+                   "form": FORMS[args.form], "l2": "inputs larger than L2 (%d MiB per array pair)"
+                   % (bytes_of(kind, dims, batch, esize) // 2 >> 20)
+                   if bytes_of(kind, dims, batch, esize) > 2 * 129e6 else "working set may fit L2",
                    "parallelism": "dp%d (independent batches)" % world},
-        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-                     "frac": round(achieved / hbm, 4),
-                     "traffic": args.traffic if args.traffic else (measured_traffic(cfg) if not args.batch and args.form == "plain" else None),
-                     "peak_source": peak_src,
-                     "kernel": "forward plan (%d launch%s), %.4f ms per launch" % (
-                         fwd.launches, "es" if fwd.launches > 1 else "", fwd_ms / fwd.launches),
-                     "passes": passes},
+        "roofline": roofline,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "accuracy": acc,
@@ -536,16 +570,18 @@ def tc_form_rate(kind, dims, batch, with_inv, src, mid, back, stream, G, torch, 
                     "tensor-pipe utilisation in profiles/line_fft_256_cols_tc_c4.md"}
 
 
-def e2e_rate(args, kind, dims, batch, src, G, torch, world):
+def e2e_rate(args, kind, dims, batch, src, G, torch, world, form=None, dtype=None):
     """Same metric through the C ABI's synchronous calls with pinned host
     buffers: every call copies its input to the device and its result back."""
-    fwd = G.BatchPlan(kind, dims, batch)
-    inv = G.BatchPlan("ci" if kind == "c" else "ri", dims, batch)
+    dtype = dtype or torch.float32
+    es = 8 if dtype == torch.float64 else 4
+    fwd = G.BatchPlan(kind, dims, batch, form=form)
+    inv = G.BatchPlan("ci" if kind == "c" else "ri", dims, batch, form=form)
     n = int(np.prod(dims))
     d = [x for x in dims if x != 1] or [1]
     h = (d[0] // 2 + 1) * (n // d[0])
     m = n * batch
-    pin = lambda k: torch.empty(k, dtype=torch.float32).pin_memory()
+    pin = lambda k: torch.empty(k, dtype=dtype).pin_memory()
     if kind == "c":
         a, b = pin(m), pin(m)
         a.copy_(src[0].cpu())
@@ -555,8 +591,8 @@ def e2e_rate(args, kind, dims, batch, src, G, torch, world):
         def step():
             fwd(a, b, o1, o2)
             inv(o1, o2, r1, r2)
-        h2d = 2 * (2 * m * 4)
-        d2h = 2 * (2 * m * 4)
+        h2d = 2 * (2 * m * es)
+        d2h = 2 * (2 * m * es)
     else:
         a = pin(m)
         a.copy_(src[0].cpu())
@@ -565,8 +601,8 @@ def e2e_rate(args, kind, dims, batch, src, G, torch, world):
         def step():
             fwd(a, o1, o2)
             inv(o1, o2, r1)
-        h2d = 4 * m + 8 * h * batch
-        d2h = 8 * h * batch + 4 * m
+        h2d = es * m + 2 * es * h * batch
+        d2h = 2 * es * h * batch + es * m
     steps = max(2, min(args.steps, 5))
     step()
     torch.cuda.synchronize()
@@ -593,7 +629,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
     ap.add_argument("--batch", type=int, default=0, help="override the batch (profiling a smaller case)")
-    ap.add_argument("--form", default="plain", choices=["plain", "tc"])
+    ap.add_argument("--form", default="plain", choices=["plain", "tc", "f64"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tc", action="store_true", help="skip timing the tensor-core form beside the plain one")

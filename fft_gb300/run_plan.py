@@ -1,8 +1,9 @@
 """Run one batched plan on seeded device data a few times, for profiling.
 
-    python -m fft_gb300.run_plan KIND DIMS BATCH [REPS]
+    python -m fft_gb300.run_plan KIND DIMS BATCH [REPS] [FORM]
 
-KIND is c, ci, r or ri; DIMS a JSON list such as [256,256,256].  Each
+KIND is c, ci, r or ri; DIMS a JSON list such as [256,256,256]; FORM plain
+(default), tc or f64 (double data through the FP64 kernels).  Each
 repetition launches the plan's kernels once on the CUDA default stream;
 the script synchronises at the end and prints the launches per transform.
 """
@@ -20,17 +21,19 @@ def main(argv):
         return 2
     kind, dims, batch = argv[0], json.loads(argv[1]), int(argv[2])
     reps = int(argv[3]) if len(argv) > 3 else 2
+    form = argv[4] if len(argv) > 4 else "plain"
+    dt = torch.float64 if form == "f64" else torch.float32
     n = 1
     for d in dims:
         n *= d
     h = (dims[0] // 2 + 1) * (n // dims[0])
-    plan = BatchPlan(kind, dims, batch)
+    plan = BatchPlan(kind, dims, batch, form=None if form == "plain" else form)
     g = torch.Generator(device="cuda").manual_seed(n + batch)
     nin = (h if kind == "ri" else n) * batch
     nout = (h if kind == "r" else n) * batch
-    a = torch.randn(nin, device="cuda", generator=g)
-    b = torch.randn(nin, device="cuda", generator=g)
-    oa = torch.empty(nout, device="cuda")
+    a = torch.randn(nin, device="cuda", generator=g, dtype=dt)
+    b = torch.randn(nin, device="cuda", generator=g, dtype=dt)
+    oa = torch.empty(nout, device="cuda", dtype=dt)
     ob = torch.empty_like(oa)
     for _ in range(reps):
         plan.launch(a, None if kind == "r" else b, oa, None if kind == "ri" else ob)

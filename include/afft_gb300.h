@@ -115,9 +115,12 @@ AFFT_GB300_API void afft_32_ri_transform(afft_32_ri_type* state,
  * floats (afft_alignment / sizeof(float) = 16 elements). */
 AFFT_GB300_API size_t afft_32_align_size(size_t sz);
 
-/* Replaces fft.h:48-80 (FP64).  This library implements the FP32 path only;
- * the FP64 entry points follow the ABI's "unsupported" convention: memsize
- * returns 0, create returns NULL, transform does nothing. */
+/* Replaces fft.h:48-80 (FP64): the same transforms, layouts, errors and
+ * pointer rules on double arrays, computed in FP64 by the library's FP64
+ * kernels (twiddles computed in FP64, never rounded).  A plan made by an
+ * afft_64_*_create (or a batched plan with AFFT_GB300_FORM_F64) runs only
+ * through the afft_64_* transforms, an FP32 plan only through the afft_32_*
+ * ones; a mismatch sets AFFT_GB300_EINVAL and launches nothing. */
 typedef struct afft_64_c_struct afft_64_c_type;
 AFFT_GB300_API size_t afft_64_c_memsize(size_t ndim, const size_t* dim, int format, int impl);
 AFFT_GB300_API afft_64_c_type* afft_64_c_create(
@@ -183,6 +186,13 @@ enum { afft_gb300_c = 0, afft_gb300_ci = 1, afft_gb300_r = 2, afft_gb300_ri = 3 
  * operands, three products accumulated in FP32 in TMEM); other passes keep
  * the FP32 butterflies.  Accuracy bound: rel-L2 <= 5e-6 vs FP64. */
 enum { AFFT_GB300_FORM_TC = 0x100 };
+
+/* Form flag, OR-ed into `format` of afft_gb300_batch_memsize/_create and
+ * afft_gb300_plan_describe: double arrays and FP64 arithmetic (the batched
+ * form of the afft_64_* transforms; run it with afft_64_<kind>_transform, or
+ * with afft_gb300_transform_async passing the double pointers as float*).
+ * Not combinable with AFFT_GB300_FORM_TC, and not accepted by the queue. */
+enum { AFFT_GB300_FORM_F64 = 0x200 };
 
 /* Batched plans: `batch` transforms of the same shape, dense and back to
  * back (transform b at offset b*in_elems / b*out_elems of each array, where

@@ -17,7 +17,8 @@
  *               of the trailing dims per plane, then a half-complex inverse
  *               along dim 0 that reads only the real part of planes 0 and d0/2.
  *
- *   port32_*    FP32 scalar port of afft's own algorithm, used as the CPU
+ *   port32_*    FP32 scalar port of afft's own algorithm (port64_*: the same
+ *               on doubles), used as the CPU
  *               baseline ("port"): radix-4 decimation passes with bit-reversed
  *               twiddle order and a final radix-8 step (onedim.hpp:55-133,
  *               135-191, 312-395, 485-507), twiddles built by afft's table
@@ -74,6 +75,18 @@ int port32_execute(const port32_plan* p, const float* in_re, const float* in_im,
 int port32_execute_batch(const port32_plan* p, int64_t batch, int threads,
                          const float* in_re, const float* in_im,
                          float* out_re, float* out_im);
+
+/* FP64 port of afft: the same algorithm and API on doubles (afft_64_*). */
+typedef struct port64_plan port64_plan;
+port64_plan* port64_plan_create(int kind, int ndim, const int64_t* dims);
+void port64_plan_destroy(port64_plan* p);
+int64_t port64_plan_in_elems(const port64_plan* p);
+int64_t port64_plan_out_elems(const port64_plan* p);
+int port64_execute(const port64_plan* p, const double* in_re, const double* in_im,
+                   double* out_re, double* out_im);
+int port64_execute_batch(const port64_plan* p, int64_t batch, int threads,
+                         const double* in_re, const double* in_im,
+                         double* out_re, double* out_im);
 
 #ifdef __cplusplus
 }

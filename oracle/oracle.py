@@ -51,15 +51,16 @@ def lib():
             getattr(L, name).argtypes = [ctypes.c_int, P, ctypes.c_int, P, P, P, P]
         L.oracle64_r2c.argtypes = [ctypes.c_int, P, P, P, P]
         L.oracle64_c2r.argtypes = [ctypes.c_int, P, P, P, P]
-        L.port32_plan_create.argtypes = [ctypes.c_int, ctypes.c_int, P]
-        L.port32_plan_create.restype = P
-        L.port32_plan_destroy.argtypes = [P]
-        L.port32_plan_in_elems.argtypes = [P]
-        L.port32_plan_in_elems.restype = I64
-        L.port32_plan_out_elems.argtypes = [P]
-        L.port32_plan_out_elems.restype = I64
-        L.port32_execute.argtypes = [P, P, P, P, P]
-        L.port32_execute_batch.argtypes = [P, I64, ctypes.c_int, P, P, P, P]
+        for pre in ("port32", "port64"):
+            getattr(L, pre + "_plan_create").argtypes = [ctypes.c_int, ctypes.c_int, P]
+            getattr(L, pre + "_plan_create").restype = P
+            getattr(L, pre + "_plan_destroy").argtypes = [P]
+            getattr(L, pre + "_plan_in_elems").argtypes = [P]
+            getattr(L, pre + "_plan_in_elems").restype = I64
+            getattr(L, pre + "_plan_out_elems").argtypes = [P]
+            getattr(L, pre + "_plan_out_elems").restype = I64
+            getattr(L, pre + "_execute").argtypes = [P, P, P, P, P]
+            getattr(L, pre + "_execute_batch").argtypes = [P, I64, ctypes.c_int, P, P, P, P]
         _lib = L
     return _lib
 
@@ -148,34 +149,45 @@ def oracle64(kind, dims, a, b=None):
 class Port32:
     """FP32 port of afft (CPU baseline).  Dense batches of one shape."""
 
+    PREFIX = "port32"
+    DTYPE = np.float32
+
     def __init__(self, kind, dims):
         self.kind = kind
         self.dims = list(dims)
         d = _dims(dims)
-        self._h = lib().port32_plan_create(KINDS[kind], len(d), _p(d))
+        self._fn = lambda name: getattr(lib(), self.PREFIX + "_" + name)
+        self._h = self._fn("plan_create")(KINDS[kind], len(d), _p(d))
         if not self._h:
             raise ValueError("invalid shape %r" % (dims,))
-        self.in_elems = lib().port32_plan_in_elems(self._h)
-        self.out_elems = lib().port32_plan_out_elems(self._h)
+        self.in_elems = self._fn("plan_in_elems")(self._h)
+        self.out_elems = self._fn("plan_out_elems")(self._h)
 
     def __del__(self):
         h = getattr(self, "_h", None)
         if h:
-            lib().port32_plan_destroy(h)
+            self._fn("plan_destroy")(h)
             self._h = None
 
     def __call__(self, a, b=None, batch=1, threads=1, out=None):
-        a = np.ascontiguousarray(a, np.float32).ravel()
-        b = None if b is None else np.ascontiguousarray(b, np.float32).ravel()
+        a = np.ascontiguousarray(a, self.DTYPE).ravel()
+        b = None if b is None else np.ascontiguousarray(b, self.DTYPE).ravel()
         if out is None:
-            ore = np.empty(batch * self.out_elems, np.float32)
-            oim = None if self.kind == "ri" else np.empty(batch * self.out_elems, np.float32)
+            ore = np.empty(batch * self.out_elems, self.DTYPE)
+            oim = None if self.kind == "ri" else np.empty(batch * self.out_elems, self.DTYPE)
         else:
             ore, oim = out
-        rc = lib().port32_execute_batch(self._h, batch, threads, _p(a), _p(b), _p(ore), _p(oim))
+        rc = self._fn("execute_batch")(self._h, batch, threads, _p(a), _p(b), _p(ore), _p(oim))
         if rc:
-            raise RuntimeError("port32 failed")
+            raise RuntimeError(self.PREFIX + " failed")
         return ore if self.kind == "ri" else (ore, oim)
+
+
+class Port64(Port32):
+    """FP64 port of afft (the CPU baseline of the afft_64_* path)."""
+
+    PREFIX = "port64"
+    DTYPE = np.float64
 
 
 _ref = None

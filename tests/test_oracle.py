@@ -127,3 +127,22 @@ def test_oracle64_against_reference_fp64_outputs(golden64):
         assert err <= 1e-14, (nm, err)
         assert case["auto_vs_scalar_rel_l2"] <= 1e-14, nm
     print("worst oracle64 vs afft_64 rel-L2: %.2e" % worst)
+
+
+def test_port64_against_reference_fp64_outputs(golden64):
+    # the FP64 port (CPU baseline of the FP64 path) restates afft's double
+    # scalar backend: within FP64 roundoff, bit-identical on most cases
+    z, cases = golden64
+    identical = 0
+    for case in cases:
+        nm, kind, dims = case["name"], case["kind"], case["dims"]
+        a = z[nm + "/in0"].astype(np.float64)
+        b = z[nm + "/in1"].astype(np.float64) if nm + "/in1" in z else None
+        ref = z[nm + "/scalar0"] if kind == "ri" else (z[nm + "/scalar0"], z[nm + "/scalar1"])
+        got = O.Port64(kind, dims)(a, b)
+        assert O.rel_l2(got, ref) <= 1e-14, nm
+        gg = got if isinstance(got, tuple) else (got,)
+        rr = ref if isinstance(ref, tuple) else (ref,)
+        identical += all(np.array_equal(x, y) for x, y in zip(gg, rr))
+    assert identical >= len(cases) // 2, identical
+    print("port64 bit-identical to afft_64 scalar on %d of %d cases" % (identical, len(cases)))
