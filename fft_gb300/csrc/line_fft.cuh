@@ -379,12 +379,14 @@ __device__ __forceinline__ void r2c_half_body(const LineParams& p, long long cta
   if (active) {
     const long long base = line_off(p.in, q);
     const long long half = (long long)Lh * p.in.es;
+    const long long S = (long long)T * p.in.es;
+    const float* pr = p.in.re + base + (long long)t * p.in.es;
+    const float* pi = p.in.im + base + (long long)t * p.in.es;
 #pragma unroll
     for (int e = 0; e < E; e++) {
       const int j = t + T * e;
-      const long long a0 = base + (long long)j * p.in.es;
-      const float2 x0 = make_float2(__ldg(p.in.re + a0), __ldg(p.in.im + a0));
-      const float2 x1 = make_float2(__ldg(p.in.re + a0 + half), __ldg(p.in.im + a0 + half));
+      const float2 x0 = make_float2(__ldg(pr + e * S), __ldg(pi + e * S));
+      const float2 x1 = make_float2(__ldg(pr + e * S + half), __ldg(pi + e * S + half));
       v[e] = h ? cmul(csub(x0, x1), ldg2(p.rtw + 2 * j)) : cadd(x0, x1);
     }
   } else {
@@ -402,6 +404,9 @@ __device__ __forceinline__ void r2c_half_body(const LineParams& p, long long cta
   line_sync<WARP_ONLY>();
   if (active) {
     const long long base = line_off(p.out, q);
+    const long long S2 = 2LL * T * p.out.es;
+    float* pr = p.out.re + base + (long long)(2 * t + h) * p.out.es;
+    float* pi = p.out.im + base + (long long)(2 * t + h) * p.out.es;
 #pragma unroll
     for (int e = 0; e < E; e++) {
       const int m = t + T * e;
@@ -420,9 +425,8 @@ __device__ __forceinline__ void r2c_half_body(const LineParams& p, long long cta
         const float2 d = make_float2(0.5f * (s0.x - s1.x), 0.5f * (s0.y + s1.y));
         x = cadd(a, cmul_negi(cmul(d, w)));
       }
-      const long long a = base + (long long)k * p.out.es;
-      p.out.re[a] = x.x;
-      p.out.im[a] = x.y;
+      pr[e * S2] = x.x;
+      pi[e * S2] = x.y;
     }
   }
 }
@@ -469,11 +473,11 @@ __device__ __forceinline__ void r2c_paired_body(const LineParams& p, long long c
   float2 v[E];
   {
     const long long base = line_off(p.in, q);
+    const long long S = (long long)T * p.in.es;
+    const float* pr = p.in.re + base + (long long)t * p.in.es;
+    const float* pi = p.in.im + base + (long long)t * p.in.es;
 #pragma unroll
-    for (int e = 0; e < E; e++) {
-      const long long ad = base + (long long)(t + T * e) * p.in.es;
-      v[e] = make_float2(__ldg(p.in.re + ad), __ldg(p.in.im + ad));
-    }
+    for (int e = 0; e < E; e++) v[e] = make_float2(__ldg(pr + e * S), __ldg(pi + e * S));
   }
   run_stages<LOGL, C, true, false, 0>(v, t, c, p.tw, sm);
 
@@ -482,6 +486,9 @@ __device__ __forceinline__ void r2c_paired_body(const LineParams& p, long long c
   for (int e = 0; e < E; e++) sm.put(c, t + T * e, v[e]);
   __syncthreads();
   const long long base = line_off(p.out, q);
+  const long long SO = (long long)T * p.out.es;
+  float* por = p.out.re + base + (long long)t * p.out.es;
+  float* poi = p.out.im + base + (long long)t * p.out.es;
 #pragma unroll
   for (int e = 0; e < E; e++) {
     const int k2 = t + T * e;
@@ -500,9 +507,8 @@ __device__ __forceinline__ void r2c_paired_body(const LineParams& p, long long c
       const float2 d = make_float2(0.5f * (s0.x - s1.x), 0.5f * (s0.y + s1.y));
       x = cadd(ha, cmul_negi(cmul(d, w)));
     }
-    const long long ad = base + (long long)k2 * p.out.es;
-    p.out.re[ad] = x.x;
-    p.out.im[ad] = x.y;
+    por[e * SO] = x.x;
+    poi[e * SO] = x.y;
   }
 }
 
@@ -533,14 +539,16 @@ __device__ __forceinline__ void c2r_paired_body(const LineParams& p, long long c
   {
     const long long base = line_off(p.in, q);
     const long long pbase = line_off(p.in, o * L2 + ((L2 - t2) & (L2 - 1)));
+    // element t1 = t + T e at b0 + e S, its mirror at b1 - e S
+    const long long S = (long long)T * p.in.es;
+    const long long b0 = base + (long long)t * p.in.es;
+    const long long b1 = t2 ? pbase + (long long)(L1 - 1 - t) * p.in.es : base + (long long)(L1 - t) * p.in.es;
 #pragma unroll
     for (int e = 0; e < E; e++) {
       const int t1 = t + T * e;
       const long long k = t2 + L2 * t1;
-      const long long a0 = base + (long long)t1 * p.in.es;
-      const long long a1 = t2 ? pbase + (long long)(L1 - 1 - t1) * p.in.es : base + (long long)(L1 - t1) * p.in.es;
-      const float2 s0 = make_float2(__ldg(p.in.re + a0), __ldg(p.in.im + a0));
-      const float2 s1 = make_float2(__ldg(p.in.re + a1), __ldg(p.in.im + a1));
+      const float2 s0 = make_float2(__ldg(p.in.re + b0 + e * S), __ldg(p.in.im + b0 + e * S));
+      const float2 s1 = make_float2(__ldg(p.in.re + b1 - e * S), __ldg(p.in.im + b1 - e * S));
       float2 z;
       if (k == 0) {
         z = make_float2(s0.x + s1.x, s0.x - s1.x);
@@ -562,15 +570,17 @@ __device__ __forceinline__ void c2r_paired_body(const LineParams& p, long long c
   const int c2 = tid / T, tt = tid % T;
   const long long q2 = o * L2 + paired_column<C>(c2, a, L2);
   const long long base = line_off(p.out, q2);
+  const long long SO = (long long)T * p.out.es;
+  float* por = p.out.re + base + (long long)tt * p.out.es;
+  float* poi = p.out.im + base + (long long)tt * p.out.es;
   auto emit = [&](auto full) {
 #pragma unroll
     for (int e = 0; e < E; e++) {
       const int k1 = tt + T * e;
       float2 x = cmul(sm.get(c2, k1), fourstep_twiddle<L1, decltype(full)::value>(p, q2, k1));
       x = cswap(x);
-      const long long ad = base + (long long)k1 * p.out.es;
-      p.out.re[ad] = x.x;
-      p.out.im[ad] = x.y;
+      por[e * SO] = x.x;
+      poi[e * SO] = x.y;
     }
   };
   if (p.tw_full) emit(std::true_type{});
@@ -858,14 +868,16 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
     }
     if (staged) {
     } else if (active) {
+      // bin i = t + T e at p0 + e S, its mirror L - i at p1 - e S
       const long long base = line_off(p.in, q);
+      const long long S = (long long)T * p.in.es;
+      const long long o0 = base + (long long)t * p.in.es, o1 = base + (long long)(L - t) * p.in.es;
+      const float *p0r = p.in.re + o0, *p0i = p.in.im + o0, *p1r = p.in.re + o1, *p1i = p.in.im + o1;
 #pragma unroll
       for (int e = 0; e < E; e++) {
         const int i = t + T * e;
-        const long long a0 = base + (long long)i * p.in.es;
-        const long long a1 = base + (long long)(L - i) * p.in.es;
-        float2 s0 = make_float2(__ldg(p.in.re + a0), __ldg(p.in.im + a0));
-        float2 s1 = make_float2(__ldg(p.in.re + a1), __ldg(p.in.im + a1));
+        float2 s0 = make_float2(__ldg(p0r + e * S), __ldg(p0i + e * S));
+        float2 s1 = make_float2(__ldg(p1r - e * S), __ldg(p1i - e * S));
         float2 z;
         if (i == 0) {
           z = make_float2(s0.x + s1.x, s0.x - s1.x);
@@ -927,11 +939,14 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
           for (int e = 0; e < E; e++) v[e] = make_float2(__ldg(pz + 2 * (t + T * e)), __ldg(pz + 2 * (t + T * e) + 1));
         }
       } else {
+        // per-thread line pointers and one warp-uniform stride between a
+        // thread's elements (T * es), so each element costs one uniform
+        // multiple instead of a 64-bit multiply-add per array
+        const long long S = (long long)T * p.in.es;
+        const float* pr = p.in.re + base + (long long)t * p.in.es;
+        const float* pi = p.in.im + base + (long long)t * p.in.es;
 #pragma unroll
-        for (int e = 0; e < E; e++) {
-          const long long a = base + (long long)(t + T * e) * p.in.es;
-          v[e] = make_float2(__ldg(p.in.re + a), __ldg(p.in.im + a));
-        }
+        for (int e = 0; e < E; e++) v[e] = make_float2(__ldg(pr + e * S), __ldg(pi + e * S));
       }
       if (p.inverse) {
 #pragma unroll
@@ -961,21 +976,30 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
         const bool inv = p.inverse;
         // one branch-free loop per case, so the twiddle loads issue together
         // tw: 0 none, 1 matrix table, 2 hi/lo pair
-        auto emit = [&](auto tw) {
+        // the four-step passes store with unit element stride: compile-time
+        // offsets from one pointer per array; other strides as the loads
+        const long long S = (long long)T * p.out.es;
+        float* pr = p.out.re + base + (long long)t2 * p.out.es;
+        float* pi = p.out.im + base + (long long)t2 * p.out.es;
+        auto emit = [&](auto tw, auto unit) {
           constexpr int TW = decltype(tw)::value;
 #pragma unroll
           for (int e = 0; e < E; e++) {
             float2 x = sm.get(c2, t2 + T * e);
             if constexpr (TW) x = cmul(x, fourstep_twiddle<L, TW == 1>(p, q2, t2 + T * e));
             x = inv ? cswap(x) : x;
-            const long long a = base + (long long)(t2 + T * e) * p.out.es;
-            p.out.re[a] = x.x;
-            p.out.im[a] = x.y;
+            const long long o = decltype(unit)::value ? (long long)(T * e) : e * S;
+            pr[o] = x.x;
+            pi[o] = x.y;
           }
         };
-        if (!p.tw_n) emit(std::integral_constant<int, 0>{});
-        else if (p.tw_full) emit(std::integral_constant<int, 1>{});
-        else emit(std::integral_constant<int, 2>{});
+        auto emit_tw = [&](auto unit) {
+          if (!p.tw_n) emit(std::integral_constant<int, 0>{}, unit);
+          else if (p.tw_full) emit(std::integral_constant<int, 1>{}, unit);
+          else emit(std::integral_constant<int, 2>{}, unit);
+        };
+        if (p.out.es == 1) emit_tw(std::true_type{});
+        else emit_tw(std::false_type{});
       }
     } else {
       // four-step twiddles only occur in cols passes
@@ -1029,11 +1053,13 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
             }
           }
         } else {
+          const long long S = (long long)T * p.out.es;
+          float* pr = p.out.re + base + (long long)t * p.out.es;
+          float* pi = p.out.im + base + (long long)t * p.out.es;
 #pragma unroll
           for (int e = 0; e < E; e++) {
-            const long long a = base + (long long)(t + T * e) * p.out.es;
-            p.out.re[a] = v[e].x;
-            p.out.im[a] = v[e].y;
+            pr[e * S] = v[e].x;
+            pi[e * S] = v[e].y;
           }
         }
       }
@@ -1050,11 +1076,13 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
     }
     if (!staged_out && active) {
       const long long base = line_off(p.out, q);
+      const long long S = (long long)T * p.out.es;
+      float* pr = p.out.re + base + (long long)t * p.out.es;
+      float* pi = p.out.im + base + (long long)t * p.out.es;
 #pragma unroll
       for (int e = 0; e < E; e++) {
-        const long long a = base + (long long)(t + T * e) * p.out.es;
-        p.out.re[a] = v[e].x;
-        p.out.im[a] = v[e].y;
+        pr[e * S] = v[e].x;
+        pi[e * S] = v[e].y;
       }
     }
   } else {
@@ -1108,6 +1136,9 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
     } else {
       if (active) {
         const long long base = line_off(p.out, q);
+        const long long S = (long long)T * p.out.es;
+        float* pr = p.out.re + base + (long long)t * p.out.es;
+        float* pi = p.out.im + base + (long long)t * p.out.es;
 #pragma unroll
         for (int e = 0; e < E; e++) {
           const int k = t + T * e;
@@ -1126,9 +1157,8 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
             const float2 b = cmul(d, w);
             x = cadd(a, cmul_negi(b));
           }
-          const long long a = base + (long long)k * p.out.es;
-          p.out.re[a] = x.x;
-          p.out.im[a] = x.y;
+          pr[e * S] = x.x;
+          pi[e * S] = x.y;
         }
       }
     }
