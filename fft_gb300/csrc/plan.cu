@@ -653,14 +653,15 @@ std::unique_ptr<Plan> build_plan(int kind, int ndim, const long long* dims, long
       // the paired pass A runs over the shorter half by default (the longer
       // one when tuned so, where its kernel exists: pass A lengths <= 512)
       const int l1p = b.tune.split ? (logl + 1) / 2 : logl / 2;
-      if (!b.f64 && logl <= 19 && b.tune.real_inv == 0 && l1p <= 9) {
+      if (!b.f64 && logl <= 18 && b.tune.real_inv == 0 && l1p <= 9) {
         // inverse four-step pass A over mirrored column pairs with the real
         // pre-pass fused into its loads (twiddle, transposing store into
         // scratch), then pass B into dst's interleaved view.  Pass A takes
         // the shorter half, L1 <= 512: tiles of 16 lines, so each mirrored
         // half-tile is a 32-byte row segment (8-line tiles of the longer
         // lengths leave 16-byte halves, measured slower than the unfused
-        // form below)
+        // form below).  Up to n = 2^19: at 2^20 the unfused form measured
+        // faster on GB300 (64 x 2^20: 0.369 vs 0.384 ms)
         const int l1 = l1p, l2 = logl - l1;
         const long long L1 = 1LL << l1, L2 = 1LL << l2;
         View S = split_view(B_SCR, B_SCR, 0);

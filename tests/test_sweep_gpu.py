@@ -39,3 +39,18 @@ def test_sweep(dims, dev):
         got = run_plan(kind, dims, a, b, dev, fmt=fmt)
         err = O.rel_l2(got, O.oracle64(kind, dims, a, b))
         assert err <= TOL, (kind, dims, fmt, err)
+
+
+@pytest.mark.parametrize("dims", SHAPES[::2], ids=lambda d: "x".join(map(str, d)))
+def test_sweep_f64(dims, dev):
+    # the same shapes through the FP64 transforms (afft_64_*), FP64 bound
+    from test_f64_gpu import TOL64, run64
+    n = int(np.prod(dims))
+    for i, kind in enumerate(("c", "ci", "r", "ri")):
+        fmt = G.afft_interleaved if (n + i) % 3 == 1 else G.afft_split
+        a, b = inputs(kind, dims, n + i)
+        a = np.asarray(a, np.float64)
+        b = None if b is None else np.asarray(b, np.float64)
+        got = run64(kind, dims, a, b, dev, fmt=fmt)
+        err = O.rel_l2(got, O.oracle64(kind, dims, a, b))
+        assert err <= TOL64, (kind, dims, fmt, err)
