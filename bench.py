@@ -263,6 +263,54 @@ def cpu_port_rate(kind, dims, batch_total, threads, budget_s, f64=False):
         threads
 
 
+def cpu_mixed_rate(items, threads, budget_s, seed=0):
+    """GFLOP/s of the oracle's FP32 port of afft over a bounded random sample
+    of the mixed batch (each transform its own call, spread over `threads`
+    host threads)."""
+    from concurrent.futures import ThreadPoolExecutor
+    from oracle import oracle as O
+    from fft_gb300 import uneven as U
+    rng = np.random.default_rng(seed)
+    order = [int(j) for j in rng.permutation(len(items))]
+    plans, work = {}, []
+    nbytes = 0
+
+    def add(j):
+        nonlocal nbytes
+        kind, dims = items[j]
+        key = (kind, tuple(dims))
+        if key not in plans:
+            plans[key] = O.Port32(kind, dims)
+        i, _ = U.elems(kind, dims)
+        a = rng.standard_normal(i).astype(np.float32)
+        b = None if kind == "r" else rng.standard_normal(i).astype(np.float32)
+        nbytes += U.bytes_moved(kind, dims)
+        work.append((plans[key], a, b, U.flops(kind, dims)))
+
+    pool = ThreadPoolExecutor(threads)
+
+    def run():
+        t0 = time.perf_counter()
+        list(pool.map(lambda w: w[0](w[1], w[2]), work))
+        return time.perf_counter() - t0
+    # grow the sample until one pass takes >= budget/4 (or 2 GB of data, or all)
+    while True:
+        for j in order[len(work):len(work) + 64]:
+            add(j)
+        dt = run()
+        if dt >= budget_s / 4 or nbytes > 2e9 or len(work) >= len(items):
+            break
+    reps = max(1, int(budget_s / max(dt, 1e-6)))
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        run()
+    dt = time.perf_counter() - t0
+    pool.shutdown()
+    fl = sum(w[3] for w in work) * reps
+    return fl / dt / 1e9, "%d of %d transforms (random sample, seed %d) x %d reps, %.1f s" % (
+        len(work), len(items), seed, reps, dt), threads
+
+
 def run_reference(args, cfg):
     world, rank, _ = dist_env()
     kind, dims, batch, desc, _ = CONFIGS[cfg]
@@ -276,7 +324,11 @@ def run_reference(args, cfg):
     sample_desc = ""
     f64 = args.form == "f64"
     for i in range(args.warmup + args.steps):
-        r, sample_desc, threads_used = cpu_port_rate(kind, dims, batch, threads, budget_s=1.5, f64=f64)
+        if kind == "queue":
+            from fft_gb300 import uneven as U
+            r, sample_desc, threads_used = cpu_mixed_rate(U.uneven_batch(batch, seed=5), threads, budget_s=1.5)
+        else:
+            r, sample_desc, threads_used = cpu_port_rate(kind, dims, batch, threads, budget_s=1.5, f64=f64)
         if i >= args.warmup:
             rates.append(r)
     value = statistics.median(rates)
@@ -298,7 +350,7 @@ def run_queue(args, desc):
     from fft_gb300 import uneven as U
     dev = torch.device("cuda", 0)
     items = U.uneven_batch(args.batch or 10000, seed=5)
-    buf, offs = U.allocate(items, dev)
+    buf, offs, boundary = U.allocate(items, dev, io_regions=True)
     q = G.Queue(U.descs(items, buf, offs), form=None if args.form == "plain" else args.form)
     stream = torch.cuda.Stream(device=dev)
     for _ in range(max(args.warmup, 3)):
@@ -359,6 +411,38 @@ def run_queue(args, desc):
               "note": "tcgen05 DFT-16 stages where eligible (radix-16 stages of 256- and 4096-point passes), "
                       "FP16 hi+lo operands, FP32 accumulation in TMEM; other passes plain FP32"}
         del qt, snap
+
+    # end to end: every step copies all inputs from pinned host memory, runs
+    # the queue and copies all outputs back (one copy each way: the inputs
+    # and the outputs occupy two contiguous regions)
+    e2e = None
+    if not args.no_e2e:
+        in_host = torch.empty(boundary, dtype=torch.float32).pin_memory()
+        out_host = torch.empty(buf.numel() - boundary, dtype=torch.float32).pin_memory()
+        in_host.copy_(buf[:boundary])
+        steps = max(2, min(args.steps, 3))
+
+        def e2e_step():
+            with torch.cuda.stream(stream):
+                buf[:boundary].copy_(in_host, non_blocking=True)
+            q.run(stream)
+            with torch.cuda.stream(stream):
+                out_host.copy_(buf[boundary:], non_blocking=True)
+        e2e_step()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            e2e_step()
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) / steps
+        e2e = {"value": round(fl / dt / 1e9, 2), "unit": "GFLOP/s", "h2d_bytes_per_step": 4 * boundary,
+               "d2h_bytes_per_step": 4 * (buf.numel() - boundary), "steps": steps,
+               "ms_per_step": round(dt * 1e3, 3)}
+        del in_host, out_host
+    cpu = None
+    if not args.no_cpu:
+        rate, sample, used = cpu_mixed_rate(items, os.cpu_count() or 1, args.cpu_budget)
+        cpu = {"value": round(rate, 3), "unit": "GFLOP/s", "cores": used, "kind": "port", "sample": sample}
     line = {
         "metric": "GFLOP/s (5N·log2N) & HBM GB/s: TC-split+batched vs plain FP32 at rel-L2≤5e-6",
         "value": round(fl / (ms / 1e3) / 1e9, 2), "unit": "GFLOP/s", "n_gpus": 1, "steps": args.steps,
@@ -369,7 +453,7 @@ def run_queue(args, desc):
         "roofline": {"bound": "hbm", "achieved": round(by / (ms / 1e3) / 1e9, 1), "peak": hbm, "unit": "GB/s",
                      "frac": round(by / (ms / 1e3) / 1e9 / hbm, 4), "traffic": args.traffic,
                      "peak_source": peak_src, "kernel": "whole queue (graph of %d launches)" % q.launches},
-        "cpu_baseline": None, "e2e": None, "tc_split_form": tc, "gpu_launches": q.launches * args.steps,
+        "cpu_baseline": cpu, "e2e": e2e, "tc_split_form": tc, "gpu_launches": q.launches * args.steps,
         "clocks": dict(clk.summary(), window="soak %.1f s + timed region" % args.soak),
     }
     print(json.dumps(line), flush=True)

@@ -48,25 +48,45 @@ def bytes_moved(kind, dims):
     return 4 * i * (2 if ci else 1) + 4 * o * (2 if co else 1)
 
 
-def allocate(items, dev, seed=0):
+def allocate(items, dev, seed=0, io_regions=False):
     """One device allocation holding every transform's input and output
-    arrays (each 256-byte aligned), inputs standard normal."""
+    arrays (each 256-byte aligned), inputs standard normal.  With io_regions
+    every input array comes first and every output array after them, so one
+    copy moves all inputs and one all outputs; the boundary (in floats) is
+    returned as a third value."""
     import torch
     align = 64
     offs = []
     total = 0
-    for kind, dims in items:
-        i, o = elems(kind, dims)
-        rec = []
-        for m in (i, i if kind != "r" else 0, o, o if kind != "ri" else 0):
-            rec.append(total if m else None)
-            total += (m + align - 1) // align * align
-        offs.append(rec)
+    pad = lambda m: (m + align - 1) // align * align
+    if io_regions:
+        for kind, dims in items:
+            i, _ = elems(kind, dims)
+            rec = []
+            for m in (i, i if kind != "r" else 0):
+                rec.append(total if m else None)
+                total += pad(m)
+            offs.append(rec)
+        boundary = total
+        for (kind, dims), rec in zip(items, offs):
+            _, o = elems(kind, dims)
+            for m in (o, o if kind != "ri" else 0):
+                rec.append(total if m else None)
+                total += pad(m)
+    else:
+        for kind, dims in items:
+            i, o = elems(kind, dims)
+            rec = []
+            for m in (i, i if kind != "r" else 0, o, o if kind != "ri" else 0):
+                rec.append(total if m else None)
+                total += pad(m)
+            offs.append(rec)
+        boundary = None
     buf = torch.empty(total, dtype=torch.float32, device=dev)
     g = torch.Generator(device=dev)
     g.manual_seed(seed)
     buf.normal_(generator=g)
-    return buf, offs
+    return (buf, offs, boundary) if io_regions else (buf, offs)
 
 
 def descs(items, buf, offs):
