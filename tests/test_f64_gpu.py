@@ -193,3 +193,18 @@ def test_f64_plans_describe_and_count(dev):
     assert p.launches == 3
     d = G.describe("c", [8192], 1, G.FORM_F64)
     assert d["f64"] == 1 and len(d["ops"]) == 1
+
+
+def test_misaligned_f64_pointers_are_refused(dev):
+    # double arrays off an 8-byte boundary are reported before any launch
+    L = G.lib()
+    p64 = G.complex_transform([64], bits=64)
+    x = torch.zeros(1024, dtype=torch.float64, device=dev)   # 8 KB: every array below fits inside
+    P = ctypes.c_void_p
+    base = x.data_ptr()
+    L.afft_64_c_transform(P(p64.state), P(base + 4), P(base + 1028), P(base + 2052), P(base + 3076))
+    code, msg = G.last_error()
+    assert code == 1 and "8-byte aligned" in msg
+    L.afft_64_c_transform(P(p64.state), P(base), P(base + 1024), P(base + 2048), P(base + 3072))
+    assert G.last_error()[0] == 0
+    torch.cuda.synchronize()
