@@ -1,0 +1,30 @@
+"""The benchmark's reference arm runs on the host alone (the oracle's port of
+afft on all host threads) and prints the one JSON line the bench contract
+asks for; checked here without a GPU."""
+import json
+import os
+import subprocess
+import sys
+
+import pytest
+
+from conftest import ROOT
+
+REQUIRED = ("metric", "value", "unit", "n_gpus", "steps", "warmup", "higher_is_better", "scaling", "vs_baseline",
+            "dtype", "data", "config", "impl", "cpu_baseline", "e2e")
+
+
+@pytest.mark.parametrize("args", [[], ["--form", "f64"], ["--config", "c3b"]], ids=["c2", "c2-f64", "c3b"])
+def test_reference_arm_line(args):
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
+                        "--warmup", "0"] + args, capture_output=True, text=True, timeout=300, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.strip()]
+    assert len(lines) == 1, r.stdout
+    d = json.loads(lines[0])
+    for k in REQUIRED:
+        assert k in d, k
+    assert d["impl"] == "reference" and d["value"] > 0 and d["unit"] == "GFLOP/s"
+    assert d["e2e"]["value"] == d["value"] and d["e2e"]["h2d_bytes_per_step"] == 0
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    assert d["dtype"] == ("f64" if "f64" in args else "f32")
