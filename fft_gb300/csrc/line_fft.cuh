@@ -110,6 +110,28 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
 }
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// The butterflies' add / subtract: with PK one packed FP32x2 instruction each
+// (sm_100+; per component the same IEEE round-to-nearest result as the scalar
+// form).  Elsewhere adds stay scalar, so multiplies feeding them still
+// contract into FMAs.
+template <bool PK>
+__device__ __forceinline__ float2 badd(float2 a, float2 b) {
+  if constexpr (PK) return __fadd2_rn(a, b);
+  else return cadd(a, b);
+}
+template <bool PK>
+__device__ __forceinline__ float2 bsub(float2 a, float2 b) {
+  if constexpr (PK) return __fadd2_rn(a, make_float2(-b.x, -b.y));
+  else return csub(a, b);
+}
+// Which line kernels take the packed butterflies, measured per length on
+// GB300: rows of 256 to 8192 points 1.3-2.5% faster, 256-, 1024- and
+// 2048-point cols passes 1-5% faster; the warp-staged rows of up to 128
+// points (6-9%) and the 512-point cols passes (2-3%) slower.
+template <int LOGL, bool COLS>
+constexpr bool packed_bfly() {
+  return COLS ? LOGL != 9 : LOGL >= 8;
+}
 __device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
 __device__ __forceinline__ float2 cmul_negi(float2 a) { return make_float2(a.y, -a.x); }   // -i*a
 __device__ __forceinline__ float2 cswap(float2 a) { return make_float2(a.y, a.x); }
@@ -132,53 +154,55 @@ __device__ __forceinline__ float2 w16(float2 a) {
   else return a;  // unused
 }
 
+template <bool PK>
 __device__ __forceinline__ void dft2(float2& a, float2& b) {
   float2 t = a;
-  a = cadd(t, b);
-  b = csub(t, b);
+  a = badd<PK>(t, b);
+  b = bsub<PK>(t, b);
 }
 
 // in-place DFT-4 on (a0, a1, a2, a3), natural order out
+template <bool PK>
 __device__ __forceinline__ void dft4(float2& a0, float2& a1, float2& a2, float2& a3) {
-  float2 s02 = cadd(a0, a2), d02 = csub(a0, a2);
-  float2 s13 = cadd(a1, a3), d13 = csub(a1, a3);
-  a0 = cadd(s02, s13);
-  a2 = csub(s02, s13);
-  a1 = cadd(d02, cmul_negi(d13));
-  a3 = csub(d02, cmul_negi(d13));
+  float2 s02 = badd<PK>(a0, a2), d02 = bsub<PK>(a0, a2);
+  float2 s13 = badd<PK>(a1, a3), d13 = bsub<PK>(a1, a3);
+  a0 = badd<PK>(s02, s13);
+  a2 = bsub<PK>(s02, s13);
+  a1 = badd<PK>(d02, cmul_negi(d13));
+  a3 = bsub<PK>(d02, cmul_negi(d13));
 }
 
-template <int R>
+template <int R, bool PK = false>
 __device__ __forceinline__ void dft(float2 (&x)[R]) {
   if constexpr (R == 1) {
   } else if constexpr (R == 2) {
-    dft2(x[0], x[1]);
+    dft2<PK>(x[0], x[1]);
   } else if constexpr (R == 4) {
-    dft4(x[0], x[1], x[2], x[3]);
+    dft4<PK>(x[0], x[1], x[2], x[3]);
   } else if constexpr (R == 8) {
     // 2 x 4: E = DFT4(even), O = DFT4(odd) * W8^k
-    dft4(x[0], x[2], x[4], x[6]);
-    dft4(x[1], x[3], x[5], x[7]);
+    dft4<PK>(x[0], x[2], x[4], x[6]);
+    dft4<PK>(x[1], x[3], x[5], x[7]);
     x[3] = w16<2>(x[3]);
     x[5] = w16<4>(x[5]);
     x[7] = w16<6>(x[7]);
     float2 y[8];
-    y[0] = cadd(x[0], x[1]); y[4] = csub(x[0], x[1]);
-    y[1] = cadd(x[2], x[3]); y[5] = csub(x[2], x[3]);
-    y[2] = cadd(x[4], x[5]); y[6] = csub(x[4], x[5]);
-    y[3] = cadd(x[6], x[7]); y[7] = csub(x[6], x[7]);
+    y[0] = badd<PK>(x[0], x[1]); y[4] = bsub<PK>(x[0], x[1]);
+    y[1] = badd<PK>(x[2], x[3]); y[5] = bsub<PK>(x[2], x[3]);
+    y[2] = badd<PK>(x[4], x[5]); y[6] = bsub<PK>(x[4], x[5]);
+    y[3] = badd<PK>(x[6], x[7]); y[7] = bsub<PK>(x[6], x[7]);
 #pragma unroll
     for (int i = 0; i < 8; i++) x[i] = y[i];
   } else if constexpr (R == 16) {
     // n = n1 + 4 n2, k = k2 + 4 k1
 #pragma unroll
-    for (int n1 = 0; n1 < 4; n1++) dft4(x[n1], x[n1 + 4], x[n1 + 8], x[n1 + 12]);
+    for (int n1 = 0; n1 < 4; n1++) dft4<PK>(x[n1], x[n1 + 4], x[n1 + 8], x[n1 + 12]);
     // now x[n1 + 4 k2] = Y[n1][k2]; twiddle W16^{n1 k2}
     x[5] = w16<1>(x[5]);  x[9] = w16<2>(x[9]);   x[13] = w16<3>(x[13]);
     x[6] = w16<2>(x[6]);  x[10] = w16<4>(x[10]); x[14] = w16<6>(x[14]);
     x[7] = w16<3>(x[7]);  x[11] = w16<6>(x[11]); x[15] = w16<9>(x[15]);
 #pragma unroll
-    for (int k2 = 0; k2 < 4; k2++) dft4(x[4 * k2], x[4 * k2 + 1], x[4 * k2 + 2], x[4 * k2 + 3]);
+    for (int k2 = 0; k2 < 4; k2++) dft4<PK>(x[4 * k2], x[4 * k2 + 1], x[4 * k2 + 2], x[4 * k2 + 3]);
     // now x[4 k2 + k1] = X[k2 + 4 k1]: transpose the 4x4 index
     float2 y[16];
 #pragma unroll
@@ -257,7 +281,7 @@ __device__ __forceinline__ float2 ldg2(const float2* p) { return __ldg(p); }
 // One Stockham stage: B = E/R butterflies per thread, butterfly b = t + T*u
 // reads slots u + B*r, applies W_{NS*R}^{r*(b mod NS)}, DFT-R, and either
 // scatters to shared memory (non-last) or keeps the canonical layout (last).
-template <int R, int NS, int E, int T, bool LAST, bool TC, int NT, class SM>
+template <int R, int NS, int E, int T, bool LAST, bool TC, int NT, bool PK, class SM>
 __device__ __forceinline__ void stage(float2 (&v)[E], int t, int c, const float2* tw, const SM& sm,
                                       bool do_write, TcState* ts) {
   constexpr int B = E / R;
@@ -276,7 +300,7 @@ __device__ __forceinline__ void stage(float2 (&v)[E], int t, int c, const float2
       static_assert(E == 16, "TC form: one butterfly per thread");
       tc_dft16<NT>(x, threadIdx.x, *ts);
     } else {
-      dft<R>(x);
+      dft<R, PK>(x);
     }
     if constexpr (LAST) {
 #pragma unroll
@@ -293,7 +317,8 @@ __device__ __forceinline__ void stage(float2 (&v)[E], int t, int c, const float2
 
 // All stages; v holds the input in canonical layout on entry and the output
 // in canonical layout on exit.
-template <int LOGL, int C, bool COLS, bool WARP_ONLY, int S, bool TC = false, class SM>
+template <int LOGL, int C, bool COLS, bool WARP_ONLY, int S, bool TC = false, bool PK = packed_bfly<LOGL, COLS>(),
+          class SM>
 __device__ __forceinline__ void run_stages(float2 (&v)[Sched<LOGL>::E], int t, int c, const float2* tw,
                                            const SM& sm, TcState* ts = nullptr) {
   using Sc = Sched<LOGL>;
@@ -312,11 +337,11 @@ __device__ __forceinline__ void run_stages(float2 (&v)[Sched<LOGL>::E], int t, i
     // form writes its operand tiles there even in the last stage)
     if constexpr (S > 0 && (!LAST || TC)) line_sync<WARP_ONLY && !TC>();
     if constexpr (!LAST) {
-      stage<R, NS, E, T, false, TC, NT>(v, t, c, tw + Sc::twoff(S), sm, true, ts);
+      stage<R, NS, E, T, false, TC, NT, PK>(v, t, c, tw + Sc::twoff(S), sm, true, ts);
       line_sync<WARP_ONLY && !TC>();                   // writes visible
-      run_stages<LOGL, C, COLS, WARP_ONLY, S + 1, TC>(v, t, c, tw, sm, ts);
+      run_stages<LOGL, C, COLS, WARP_ONLY, S + 1, TC, PK>(v, t, c, tw, sm, ts);
     } else {
-      stage<R, NS, E, T, true, TC, NT>(v, t, c, tw + Sc::twoff(S), sm, false, ts);
+      stage<R, NS, E, T, true, TC, NT, PK>(v, t, c, tw + Sc::twoff(S), sm, false, ts);
     }
   }
 }
