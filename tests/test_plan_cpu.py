@@ -104,3 +104,29 @@ def test_launch_counts_f64():
     assert len(d["ops"]) == 2 and d["ops"][0]["logl"] == 11 and d["ops"][0]["C"] == 4
     assert describe("c", [256, 256, 256], 1, F)["scratch_elems"] == 0
     assert len(describe("c", [1 << 22], 1, F)["ops"]) == 2
+
+
+def test_uneven_io_regions_layout():
+    # the mixed batch's end-to-end leg copies all inputs and all outputs in
+    # one piece each: inputs below the boundary, outputs above, disjoint,
+    # every array 256-byte aligned
+    import torch
+    from fft_gb300 import uneven as U
+    items = U.uneven_batch(300, seed=3, max_log1d=12, side2d=(4, 6), side3d=(3, 4))
+    buf, offs, boundary = U.allocate(items, "cpu", io_regions=True)
+    spans = []
+    for (kind, dims), rec in zip(items, offs):
+        i, o = U.elems(kind, dims)
+        sizes = (i, i if kind != "r" else 0, o, o if kind != "ri" else 0)
+        for slot, (off, m) in enumerate(zip(rec, sizes)):
+            if not m:
+                assert off is None
+                continue
+            assert off % 64 == 0
+            assert (off + m <= boundary) if slot < 2 else (off >= boundary)
+            spans.append((off, off + m))
+    spans.sort()
+    assert all(a[1] <= b[0] for a, b in zip(spans, spans[1:]))
+    assert spans[-1][1] <= buf.numel()
+    # the same transforms and descriptors as the interleaved layout
+    assert len(U.descs(items, buf, offs)) == len(items)
