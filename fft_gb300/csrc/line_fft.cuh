@@ -127,10 +127,12 @@ __device__ __forceinline__ float2 bsub(float2 a, float2 b) {
 // Which line kernels take the packed butterflies, measured per length on
 // GB300: rows of 256 to 8192 points 1.3-2.5% faster, 256-, 1024- and
 // 2048-point cols passes 1-5% faster; the warp-staged rows of up to 128
-// points (6-9%) and the 512-point cols passes (2-3%) slower.
-template <int LOGL, bool COLS>
+// points (6-9%), the 512-point cols passes (2-3%) and the transposing-store
+// passes of 1024 points and more (the long 1D real forward's pass A, 2.4%)
+// slower.
+template <int LOGL, bool COLS, bool TSTORE = false>
 constexpr bool packed_bfly() {
-  return COLS ? LOGL != 9 : LOGL >= 8;
+  return COLS ? (LOGL != 9 && !(TSTORE && LOGL >= 10)) : LOGL >= 8;
 }
 __device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
 __device__ __forceinline__ float2 cmul_negi(float2 a) { return make_float2(a.y, -a.x); }   // -i*a
@@ -983,7 +985,7 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
     }
   }
 
-  run_stages<LOGL, C, COLS, WARP_ONLY, 0, TC>(v, t, c, p.tw, sm, ts);
+  run_stages<LOGL, C, COLS, WARP_ONLY, 0, TC, packed_bfly<LOGL, COLS, TSTORE>()>(v, t, c, p.tw, sm, ts);
 
   if constexpr (KIND == LK_C2C) {
     if constexpr (TSTORE) {
