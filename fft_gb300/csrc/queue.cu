@@ -7,9 +7,11 @@
 // are grouped by (level, kernel shape) into device-side descriptor tables;
 // each group is ONE launch (line_fft_grouped or elementwise_grouped) of one
 // CTA per virtual CTA, which finds its segment in a per-virtual-CTA map.
-// Groups of one level are independent and become parallel branches of a
-// CUDA graph; levels follow each other.  The first run captures the graph,
-// later runs replay it.
+// The first run builds a CUDA graph with one kernel node per group, which
+// depends on exactly the groups that ran the previous pass of its own
+// transforms (the transforms are independent of each other), so a pass of
+// one transform starts as soon as its own previous pass has finished; later
+// runs replay the graph.
 //
 // Scratch for transforms whose plans need it (four-step passes, real
 // inverse of N-D arrays) comes from one queue-owned arena, a disjoint region
@@ -28,6 +30,9 @@ namespace agb {
 
 struct Group {
   int level = 0;
+  int id = 0;              // index at creation (before the groups are sorted)
+  std::vector<int> trans;  // transforms with an op in this group
+  std::vector<int> preds;  // groups this one waits for (sorted indices)
   bool line = true;
   LineKernel k{};
   std::vector<Segment> segs;
@@ -47,8 +52,6 @@ struct QueueImpl {
   float* arena = nullptr;
   cudaGraphExec_t exec = nullptr;
   cudaStream_t stream = nullptr;
-  std::vector<cudaStream_t> pool;
-  std::vector<cudaEvent_t> events;
   int device = 0;
   ~QueueImpl() {
     if (exec) cudaGraphExecDestroy(exec);
@@ -57,8 +60,6 @@ struct QueueImpl {
       if (g.d_map) cudaFree(g.d_map);
     }
     if (arena) cudaFree(arena);
-    for (auto s : pool) cudaStreamDestroy(s);
-    for (auto e : events) cudaEventDestroy(e);
     if (stream) cudaStreamDestroy(stream);
   }
 };
@@ -111,8 +112,9 @@ static int build_queue(QueueImpl& Q) {
     set_error(AFFT_GB300_ENOMEM, "queue scratch allocation failed");
     return AFFT_GB300_ENOMEM;
   }
-  // segments, grouped by (level, kernel)
+  // segments, grouped by (level, kernel); tgroup[j][i] = group of op i of transform j
   std::map<std::pair<int, const void*>, size_t> gidx;
+  std::vector<std::vector<int>> tgroup(Q.descs.size());
   for (size_t j = 0; j < Q.descs.size(); j++) {
     const auto& d = Q.descs[j];
     float* base[B_NBUF] = {(float*)d.src_re, (float*)d.src_im, d.dst_re, d.dst_im,
@@ -130,12 +132,15 @@ static int build_queue(QueueImpl& Q) {
       if (it == gidx.end()) {
         Group g;
         g.level = (int)i;
+        g.id = (int)Q.groups.size();
         g.line = op.type == OP_LINE;
         g.k = op.k;
         it = gidx.emplace(key, Q.groups.size()).first;
         Q.groups.push_back(g);
       }
       Group& g = Q.groups[it->second];
+      g.trans.push_back((int)j);
+      tgroup[j].push_back((int)it->second);
       if (op.type == OP_LINE) {
         Segment s;
         s.p = op.p;
@@ -226,60 +231,45 @@ static int build_queue(QueueImpl& Q) {
   std::stable_sort(Q.groups.begin(), Q.groups.end(), [](const Group& a, const Group& b) {
     return a.level != b.level ? a.level < b.level : a.total > b.total;
   });
+  // each group waits for the groups holding the previous pass of its transforms
+  std::vector<int> pos(Q.groups.size());
+  for (size_t n = 0; n < Q.groups.size(); n++) pos[Q.groups[n].id] = (int)n;
+  for (auto& g : Q.groups) {
+    if (g.level > 0)
+      for (int j : g.trans) g.preds.push_back(pos[tgroup[j][g.level - 1]]);
+    std::sort(g.preds.begin(), g.preds.end());
+    g.preds.erase(std::unique(g.preds.begin(), g.preds.end()), g.preds.end());
+  }
   return 0;
 }
 
-static void launch_group(const Group& g, cudaStream_t st) {
-  if (g.total == 0) return;
-  if (g.line)
-    g.k.grouped<<<g.grid, g.threads, g.smem, st>>>((const Segment*)g.d_tab, g.d_map, g.total);
-  else
-    elementwise_grouped<<<g.grid, g.threads, 0, st>>>((const EwSegment*)g.d_tab, g.d_map, g.total);
-}
-
 static int capture(QueueImpl& Q) {
-  size_t width = 1;
-  for (size_t i = 0; i < Q.groups.size();) {
-    size_t j = i;
-    while (j < Q.groups.size() && Q.groups[j].level == Q.groups[i].level) j++;
-    width = std::max(width, j - i);
-    i = j;
-  }
-  width = std::min<size_t>(width, 16);
-  while (Q.pool.size() < width) {
-    cudaStream_t s;
-    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return AFFT_GB300_ECUDA;
-    Q.pool.push_back(s);
-  }
-  while (Q.events.size() < Q.groups.size() + 1) {
-    cudaEvent_t e;
-    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return AFFT_GB300_ECUDA;
-    Q.events.push_back(e);
-  }
-  cudaStream_t s0 = Q.stream;
-  if (cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return AFFT_GB300_ECUDA;
-  for (size_t i = 0; i < Q.groups.size();) {
-    size_t j = i;
-    while (j < Q.groups.size() && Q.groups[j].level == Q.groups[i].level) j++;
-    if (j - i == 1) {
-      launch_group(Q.groups[i], s0);
-    } else {
-      cudaEventRecord(Q.events.back(), s0);   // fork
-      for (size_t g = i; g < j; g++) {
-        cudaStream_t sg = Q.pool[(g - i) % Q.pool.size()];
-        cudaStreamWaitEvent(sg, Q.events.back(), 0);
-        launch_group(Q.groups[g], sg);
-        cudaEventRecord(Q.events[g], sg);
-      }
-      for (size_t g = i; g < j; g++) cudaStreamWaitEvent(s0, Q.events[g], 0);   // join
-    }
-    i = j;
-  }
+  // one node per group (an empty node for a group without work, so the
+  // dependency chain stays whole), with edges from its predecessor groups
   cudaGraph_t graph = nullptr;
-  cudaError_t e = cudaStreamEndCapture(s0, &graph);
-  if (e != cudaSuccess) return AFFT_GB300_ECUDA;
-  e = cudaGraphInstantiate(&Q.exec, graph, 0);
+  if (cudaGraphCreate(&graph, 0) != cudaSuccess) return AFFT_GB300_ECUDA;
+  std::vector<cudaGraphNode_t> node(Q.groups.size());
+  bool ok = true;
+  for (size_t n = 0; n < Q.groups.size() && ok; n++) {
+    Group& g = Q.groups[n];
+    std::vector<cudaGraphNode_t> deps;
+    for (int p : g.preds) deps.push_back(node[p]);
+    if (g.total == 0) {
+      ok = cudaGraphAddEmptyNode(&node[n], graph, deps.data(), deps.size()) == cudaSuccess;
+      continue;
+    }
+    cudaKernelNodeParams kp{};
+    void* args[3] = {&g.d_tab, &g.d_map, &g.total};
+    kp.func = g.line ? (void*)g.k.grouped : (void*)&elementwise_grouped;
+    kp.gridDim = dim3((unsigned)g.grid);
+    kp.blockDim = dim3((unsigned)g.threads);
+    kp.sharedMemBytes = (unsigned)g.smem;
+    kp.kernelParams = args;
+    ok = cudaGraphAddKernelNode(&node[n], graph, deps.data(), deps.size(), &kp) == cudaSuccess;
+  }
+  cudaError_t e = ok ? cudaGraphInstantiate(&Q.exec, graph, 0) : cudaErrorUnknown;
   cudaGraphDestroy(graph);
+  if (!ok) cudaGetLastError();
   return e == cudaSuccess ? 0 : AFFT_GB300_ECUDA;
 }
 

@@ -287,7 +287,10 @@ typedef struct afft_gb300_desc
 /* A queue runs many transforms of mixed sizes and kinds as one unit: plans
  * are made once per distinct (kind, shape), the launches of all transforms
  * are grouped by kernel and recorded into one CUDA graph on first run, and
- * each later run replays that graph.  The descriptor array is copied. */
+ * each later run replays that graph.  The descriptor array is copied.  The
+ * transforms are independent: they run in no particular order relative to
+ * each other, so no transform's output may overlap another's input or
+ * output. */
 typedef struct afft_gb300_queue afft_gb300_queue;
 AFFT_GB300_API afft_gb300_queue* afft_gb300_queue_create(const afft_gb300_desc* descs,
   size_t count);
