@@ -331,6 +331,7 @@ int afft_gb300_queue_run(afft_gb300_queue* q, void* stream) {
       if (p >= 0 && p != d) cudaSetDevice(p);
     }
   } restore{Q.device, prev};
+  if (Q.groups.empty()) return 0;   // nothing queued: no graph, no launch
   if (!Q.exec && capture(Q)) {
     cudaGetLastError();
     set_error(AFFT_GB300_ECUDA, "graph capture failed");

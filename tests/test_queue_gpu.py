@@ -73,3 +73,10 @@ def test_queue_rejects_bad_descriptors(dev):
         G.Queue([("c", [12], x, x, x, x)])
     with pytest.raises(G.AfftError):
         G.Queue([("c", [2, 2, 2, 2], x, x, x, x)])
+
+
+def test_empty_queue_runs_nothing():
+    q = G.Queue([])
+    assert q.launches == 0
+    q.run()
+    assert G.last_error()[0] == 0
