@@ -208,3 +208,16 @@ def test_misaligned_f64_pointers_are_refused(dev):
     L.afft_64_c_transform(P(p64.state), P(base), P(base + 1024), P(base + 2048), P(base + 3072))
     assert G.last_error()[0] == 0
     torch.cuda.synchronize()
+
+
+@pytest.mark.parametrize("n", [1, 2, 4])
+@pytest.mark.parametrize("batch", [1, 5])
+def test_tiny_real_f64(n, batch, dev):
+    # real transforms of total size 1 (the length-1 DFT), 2 and 4: the
+    # smallest FP64 line kernels and the size-1 elementwise kernel
+    a, _ = inputs("r", [n], batch, 11 * n + batch)
+    hr, hi = run64("r", [n], a, None, dev, batch=batch)
+    assert O.rel_l2((hr, hi), oracle_batch("r", [n], a, None, batch)) <= TOL64
+    br, bi = inputs("ri", [n], batch, 13 * n + batch)
+    y = run64("ri", [n], br, bi, dev, batch=batch)
+    assert O.rel_l2(y, oracle_batch("ri", [n], br, bi, batch)) <= TOL64
