@@ -137,6 +137,37 @@ def ptr(a):
     raise TypeError(type(a))
 
 
+def _validate(kind, dims, batch, fmt, bits, src_re, src_im, dst_re, dst_im):
+    """Check the array objects a transform call gets (numpy arrays, torch
+    tensors): element type, contiguity and size against what the transform
+    reads and writes, so that a wrong array is refused here instead of the
+    kernels reading or writing past it.  Raw int pointers are not checked."""
+    k = KINDS[kind] if isinstance(kind, str) else kind
+    d = squeeze(dims)
+    n = 1
+    for x in d:
+        n *= x
+    h = half_elems(d)
+    inter = fmt == afft_interleaved
+    cin, cout = k != KIND_R, k != KIND_RI
+    m_in = (h if k == KIND_RI else n) * batch
+    m_out = (h if k == KIND_R else n) * batch
+    want = {"src_re": m_in * (2 if cin and inter else 1), "src_im": m_in if cin and not inter else 0,
+            "dst_re": m_out * (2 if cout and inter else 1), "dst_im": m_out if cout and not inter else 0}
+    name = "float64" if bits == 64 else "float32"
+    for role, a in (("src_re", src_re), ("src_im", src_im), ("dst_re", dst_re), ("dst_im", dst_im)):
+        if a is None or isinstance(a, int) or not want[role] or not hasattr(a, "dtype"):
+            continue
+        if str(a.dtype).split(".")[-1] != name:
+            raise AfftError("%s: %s array expected, got %s" % (role, name, a.dtype))
+        size = a.numel() if hasattr(a, "numel") else a.size
+        contig = a.is_contiguous() if hasattr(a, "is_contiguous") else a.flags["C_CONTIGUOUS"]
+        if not contig:
+            raise AfftError("%s: the array must be contiguous" % role)
+        if size < want[role]:
+            raise AfftError("%s: %d elements, the transform needs %d" % (role, size, want[role]))
+
+
 def describe(kind, dims, batch=1, fmt=0):
     """The kernel launches a batched plan issues, as a dict (from
     afft_gb300_plan_describe; no device needed)."""
@@ -275,6 +306,7 @@ class complex_transform(_Plan):
     kind = KIND_C
 
     def __call__(self, src_re, src_im, dst_re, dst_im):
+        _validate(self.kind, self.dims, 1, self.format, self.bits, src_re, src_im, dst_re, dst_im)
         self._fn(self.state, ptr(src_re), ptr(src_im), ptr(dst_re), ptr(dst_im))
         _check("transform")
 
@@ -289,6 +321,7 @@ class real_transform(_Plan):
     kind = KIND_R
 
     def __call__(self, src, dst_re, dst_im):
+        _validate(self.kind, self.dims, 1, self.format, self.bits, src, None, dst_re, dst_im)
         self._fn(self.state, ptr(src), ptr(dst_re), ptr(dst_im))
         _check("transform")
 
@@ -298,6 +331,7 @@ class inverse_real_transform(_Plan):
     kind = KIND_RI
 
     def __call__(self, src_re, src_im, dst):
+        _validate(self.kind, self.dims, 1, self.format, self.bits, src_re, src_im, dst, None)
         self._fn(self.state, ptr(src_re), ptr(src_im), ptr(dst))
         _check("transform")
 
@@ -339,9 +373,15 @@ class BatchPlan:
         self._fn = getattr(L, "afft_%d_%s_transform" % (64 if form == "f64" else 32, name))
 
     def __call__(self, a, b=None, c=None, d=None):
+        bits = 64 if self.form == "f64" else 32
         if self.kind in (KIND_C, KIND_CI):
+            _validate(self.kind, self.dims, self.batch, self.format, bits, a, b, c, d)
             self._fn(self.state, ptr(a), ptr(b), ptr(c), ptr(d))
+        elif self.kind == KIND_R:
+            _validate(self.kind, self.dims, self.batch, self.format, bits, a, None, b, c)
+            self._fn(self.state, ptr(a), ptr(b), ptr(c))
         else:
+            _validate(self.kind, self.dims, self.batch, self.format, bits, a, b, c, None)
             self._fn(self.state, ptr(a), ptr(b), ptr(c))
         _check("transform")
 
@@ -349,6 +389,8 @@ class BatchPlan:
         """Enqueue without waiting; ``stream`` is a torch.cuda.Stream, a raw
         cudaStream_t int, or None for the CUDA default stream."""
         s = stream.cuda_stream if hasattr(stream, "cuda_stream") else stream
+        _validate(self.kind, self.dims, self.batch, self.format, 64 if self.form == "f64" else 32,
+                  src_re, src_im, dst_re, dst_im)
         rc = lib().afft_gb300_transform_async(self.state, ptr(src_re), ptr(src_im), ptr(dst_re), ptr(dst_im), s)
         if rc:
             _check("transform_async")

@@ -99,3 +99,24 @@ def test_release_unknown_plan():
     buf = ctypes.create_string_buffer(128)
     assert G.lib().afft_gb300_release(ctypes.addressof(buf)) == 5
     assert G.lib().afft_gb300_plan_launches(ctypes.addressof(buf)) == -1
+
+
+def test_python_front_end_checks_arrays():
+    # a wrong element type, a short array or a strided view is refused before
+    # any pointer reaches the library
+    import numpy as np
+    V = G._validate
+    f32, f64 = np.zeros(64, np.float32), np.zeros(64, np.float64)
+    V("c", [64], 1, G.afft_split, 32, f32, f32, f32, f32)
+    V("c", [64], 1, G.afft_split, 64, f64, f64, f64, f64)
+    V("r", [64], 1, G.afft_split, 32, f32, None, np.zeros(33, np.float32), np.zeros(33, np.float32))
+    V("ri", [64], 1, G.afft_interleaved, 32, np.zeros(66, np.float32), None, f32, None)
+    V("c", [64], 1, G.afft_split, 32, 12345, 12345, 12345, 12345)            # raw pointers: unchecked
+    with pytest.raises(G.AfftError, match="float64"):
+        V("c", [64], 1, G.afft_split, 64, f32, f32, f32, f32)
+    with pytest.raises(G.AfftError, match="elements"):
+        V("c", [64], 2, G.afft_split, 32, f32, f32, f32, f32)
+    with pytest.raises(G.AfftError, match="elements"):
+        V("c", [64], 1, G.afft_interleaved, 32, f32, None, f32, None)        # needs 128 per array
+    with pytest.raises(G.AfftError, match="contiguous"):
+        V("c", [32], 1, G.afft_split, 32, f32[::2], f32, f32, f32)
