@@ -192,9 +192,13 @@ def accuracy(kind, dims, batch, src, mid, back, with_inv):
     m = h if kind != "c" else n
     y = mid[0][:k * m].double().cpu().numpy() + 1j * mid[1][:k * m].double().cpu().numpy()
     ref = ref.reshape(-1)
+    # afft's own harness metric (testing.cpp:1113-1129) beside the standard ones
+    afft_metric = float(np.sqrt(np.sum(np.abs(y - ref) ** 2) / np.sum(np.abs(y) ** 2 + np.abs(ref) ** 2)))
     out = {"sample": "%d of %d transforms" % (k, batch), "reference": "numpy float64 FFT",
            "rel_l2": float(np.linalg.norm(y - ref) / np.linalg.norm(ref)),
-           "max_err": float(np.abs(y - ref).max() / np.abs(ref).max())}
+           "max_err": float(np.abs(y - ref).max() / np.abs(ref).max()),
+           "afft_metric": afft_metric,
+           "afft_bound": 1.2e-7 * math.sqrt(max(math.log2(int(np.prod(d))), 1.0))}
     if with_inv:
         xb = back[0][:k * n].double().cpu().numpy()
         if kind == "c":

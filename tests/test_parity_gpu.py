@@ -568,3 +568,28 @@ def test_batched_interleaved_complex(kind, n, batch, pad, dev):
         sl = slice(t * n, (t + 1) * n)
         ref = O.oracle64(kind, [n], a[sl], b[sl])
         assert O.rel_l2((o[0::2][sl], o[1::2][sl]), ref) <= TOL, (kind, n, batch, pad, t)
+
+
+def test_golden_cases_pass_afft_criterion(golden, dev):
+    # afft's own harness metric and pass criterion (testing.cpp:1113-1129,
+    # 1321-1331; precision 1.2e-7 as run_all.cpp:68): every GPU result passes
+    # it against the FP64 oracle; afft's own float outputs on the same inputs
+    # are measured beside it
+    import math
+    z, cases = golden
+    worst_ours = worst_afft = 0.0
+    for case in cases:
+        nm, kind, dims = case["name"], case["kind"], case["dims"]
+        if nm == "c1":
+            continue
+        a = z[nm + "/in0"]
+        b = z[nm + "/in1"] if nm + "/in1" in z else None
+        ref = O.oracle64(kind, dims, a, b)
+        bound = 1.2e-7 * math.sqrt(max(math.log2(int(np.prod(dims))), 1.0))
+        ours = O.afft_error(run_plan(kind, dims, a, b, dev), ref)
+        assert ours <= bound, (nm, ours, bound)
+        for tag in ("scalar", "auto"):
+            out = z[nm + "/%s0" % tag] if kind == "ri" else (z[nm + "/%s0" % tag], z[nm + "/%s1" % tag])
+            worst_afft = max(worst_afft, O.afft_error(out, ref) / bound)
+        worst_ours = max(worst_ours, ours / bound)
+    print("afft metric / afft bound, worst over golden cases: GPU %.3f, afft itself %.3f" % (worst_ours, worst_afft))
