@@ -461,6 +461,9 @@ def run_queue(args, desc):
     if not args.no_cpu:
         rate, sample, used = cpu_mixed_rate(items, os.cpu_count() or 1, args.cpu_budget)
         cpu = {"value": round(rate, 3), "unit": "GFLOP/s", "cores": used, "kind": "port", "sample": sample}
+        if used > 1:
+            r1, s1, _ = cpu_mixed_rate(items, 1, max(1.0, args.cpu_budget / 4))
+            cpu["single_thread"] = {"value": round(r1, 3), "cores": 1, "sample": s1}
     line = {
         "metric": "GFLOP/s (5N·log2N) & HBM GB/s: TC-split+batched vs plain FP32 at rel-L2≤5e-6",
         "value": round(fl / (ms / 1e3) / 1e9, 2), "unit": "GFLOP/s", "n_gpus": 1, "steps": args.steps,
@@ -606,6 +609,10 @@ def run_ours(args, cfg):
         threads = os.cpu_count() or 1
         rate, sample, used = cpu_port_rate(kind, dims, batch, threads, budget_s=args.cpu_budget, f64=f64)
         cpu = {"value": round(rate, 3), "unit": "GFLOP/s", "cores": used, "kind": "port", "sample": sample}
+        if used > 1:
+            # the same port on one thread (a bounded sample), beside all host threads
+            r1, s1, _ = cpu_port_rate(kind, dims, batch, 1, budget_s=max(1.0, args.cpu_budget / 4), f64=f64)
+            cpu["single_thread"] = {"value": round(r1, 3), "cores": 1, "sample": s1}
     if f64:
         # FP64 arithmetic, not HBM, bounds the FP64 kernels on GB300
         fwd_gflops = flops_of(kind, dims, batch) / (fwd_ms / 1e3) / 1e9
