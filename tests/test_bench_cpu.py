@@ -14,7 +14,8 @@ REQUIRED = ("metric", "value", "unit", "n_gpus", "steps", "warmup", "higher_is_b
             "dtype", "data", "config", "impl", "cpu_baseline", "e2e")
 
 
-@pytest.mark.parametrize("args", [[], ["--form", "f64"], ["--config", "c3b"]], ids=["c2", "c2-f64", "c3b"])
+@pytest.mark.parametrize("args", [[], ["--form", "f64"], ["--config", "c3b"], ["--config", "c5"]],
+                         ids=["c2", "c2-f64", "c3b", "c5"])
 def test_reference_arm_line(args):
     r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
                         "--warmup", "0"] + args, capture_output=True, text=True, timeout=300, cwd=ROOT)
