@@ -16,7 +16,8 @@ struct LineKernel {
   int kind;            // LK_C2C / LK_R2C / LK_C2R
   int tstore;          // store with the along-line mapping (four-step pass A)
   int tc;              // split-precision tensor-core butterflies
-  int unit;            // unit element strides specialised (rows c2c): 1 split, 2 interleaved
+  int unit;            // rows c2c: unit element strides, 1 split, 2 interleaved; cols c2c:
+                       // interleaved pairs, bit 0 input, bit 1 output
   int lines_per_cta;   // C
   int threads;         // T * C
   size_t smem;         // bytes of dynamic shared memory
@@ -33,6 +34,10 @@ bool get_line_kernel(int logl, bool cols, int kind, bool tstore, LineKernel* out
 bool get_rows_c2c_unit(int logl, bool tc, LineKernel* out);
 // rows c2c on interleaved pairs with unit pair strides (float2 accesses)
 bool get_rows_c2c_iunit(int logl, LineKernel* out);
+// cols c2c on interleaved pairs (im right after re, even element stride):
+// pairs bit 0 = input, bit 1 = output (the kernels' UNIT in cols mode), for
+// lines of 2^5 .. 2^11 points; the transposing store only with pairs = 1
+bool get_cols_c2c_pairs(int logl, bool tstore, int pairs, LineKernel* out);
 
 // FP64 kernels (line_fft64.cuh, k_f64_*.cu): rows {C2C, R2C, C2R} up to
 // 2^13 points, cols {C2C (also with the transposing store), R2C, C2R} up to

@@ -845,10 +845,11 @@ __device__ __forceinline__ void rows_stage_out_reals(const LineParams& p, long l
 }
 
 // The body of one CTA's work: lines [cta*C, cta*C + C) of the launch `p`.
-// UNIT: 1 both element strides are 1 (split complex rows), 2 both are 2 with
-// im = re + 1 (interleaved complex rows, loaded and stored as float2), so
-// element offsets are compile-time constants instead of runtime 64-bit
-// products.
+// UNIT, rows mode: 1 both element strides are 1 (split complex rows), 2 both
+// are 2 with im = re + 1 (interleaved complex rows, loaded and stored as
+// float2), so element offsets are compile-time constants instead of runtime
+// 64-bit products.  Cols mode: bit 0 the input, bit 1 the output are
+// interleaved pairs (im = re + 1, even strides), accessed as float2.
 template <int LOGL, int C, bool COLS, int KIND, bool TSTORE, bool TC = false, int UNIT = 0>
 __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta, TcState* ts = nullptr) {
   if constexpr (KIND == LK_R2C_HALF) {
@@ -868,6 +869,8 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
   }
   using Sc = Sched<LOGL>;
   constexpr int L = Sc::L, E = Sc::E, T = Sc::T;
+  constexpr int RU = COLS ? 0 : UNIT;       // rows: unit-stride variants
+  constexpr int CPAIRS = COLS ? UNIT : 0;   // cols: interleaved-pair input / output
   // a line lives inside one warp: rows mode with T <= 32, or a single line
   constexpr bool WARP_ONLY = (!COLS && T <= 32) || (T * C <= 32);
   extern __shared__ __align__(1024) float2 smem_raw[];
@@ -929,19 +932,19 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
         staged = true;
       }
     }
-    if constexpr (UNIT == 1 && !COLS && T <= AFFT_STAGE_T && E == 16 && !TC) {
+    if constexpr (RU == 1 && T <= AFFT_STAGE_T && E == 16 && !TC) {
       if (rows_contiguous(p.in, L)) {
         rows_stage_in<LOGL, C>(p, cta, sm, v, t, c);
         staged = true;
       }
     }
-    if constexpr (UNIT == 2 && !COLS && T <= AFFT_STAGE_T && E == 16 && !TC) {
+    if constexpr (RU == 2 && T <= AFFT_STAGE_T && E == 16 && !TC) {
       if (reals_contiguous(p.in, L)) {   // interleaved pairs: the same view as real rows
         rows_stage_in_reals<LOGL, C>(p, cta, sm, v, t, c);
         staged = true;
       }
     }
-    if constexpr (UNIT != 0) {
+    if constexpr (RU != 0) {
       if (staged && p.inverse) {
 #pragma unroll
         for (int e = 0; e < E; e++) v[e] = cswap(v[e]);
@@ -950,12 +953,12 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
     if (staged) {
     } else if (active) {
       const long long base = line_off(p.in, q);
-      if constexpr (UNIT == 1) {
+      if constexpr (RU == 1) {
         const float* pr = p.in.re + base + t;
         const float* pi = p.in.im + base + t;
 #pragma unroll
         for (int e = 0; e < E; e++) v[e] = make_float2(__ldg(pr + T * e), __ldg(pi + T * e));
-      } else if constexpr (UNIT == 2) {
+      } else if constexpr (RU == 2) {
         const float* pz = p.in.re + base;
         if ((reinterpret_cast<uintptr_t>(pz) & 7) == 0) {
           const float2* pp = reinterpret_cast<const float2*>(pz) + t;
@@ -972,8 +975,17 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
         const long long S = (long long)T * p.in.es;
         const float* pr = p.in.re + base + (long long)t * p.in.es;
         const float* pi = p.in.im + base + (long long)t * p.in.es;
+        // cols kernels built for interleaved input pairs (UNIT bit 0: im right
+        // after re, even stride): one 8-byte load per element where the line
+        // starts 8-byte aligned
+        if ((CPAIRS & 1) && !(reinterpret_cast<uintptr_t>(pr) & 7)) {
+          const float2* pz = reinterpret_cast<const float2*>(pr);
 #pragma unroll
-        for (int e = 0; e < E; e++) v[e] = make_float2(__ldg(pr + e * S), __ldg(pi + e * S));
+          for (int e = 0; e < E; e++) v[e] = __ldg(pz + e * (S >> 1));
+        } else {
+#pragma unroll
+          for (int e = 0; e < E; e++) v[e] = make_float2(__ldg(pr + e * S), __ldg(pi + e * S));
+        }
       }
       if (p.inverse) {
 #pragma unroll
@@ -1044,13 +1056,13 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
         for (int e = 0; e < E; e++) v[e] = cswap(v[e]);
       }
       bool staged_out = false;
-      if constexpr (UNIT == 1 && !COLS && T <= AFFT_STAGE_T && E == 16 && !TC) {
+      if constexpr (RU == 1 && T <= AFFT_STAGE_T && E == 16 && !TC) {
         if (rows_contiguous(p.out, L)) {
           rows_stage_out<LOGL, C>(p, cta, sm, v, t, c);
           staged_out = true;
         }
       }
-      if constexpr (UNIT == 2 && !COLS && T <= AFFT_STAGE_T && E == 16 && !TC) {
+      if constexpr (RU == 2 && T <= AFFT_STAGE_T && E == 16 && !TC) {
         if (reals_contiguous(p.out, L)) {
           rows_stage_out_reals<LOGL, C>(p, cta, sm, v, t, c);
           staged_out = true;
@@ -1058,7 +1070,7 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
       }
       if (!staged_out && active) {
         const long long base = line_off(p.out, q);
-        if constexpr (UNIT == 1) {
+        if constexpr (RU == 1) {
           float* pr = p.out.re + base + t;
           float* pi = p.out.im + base + t;
 #pragma unroll
@@ -1066,7 +1078,7 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
             pr[T * e] = v[e].x;
             pi[T * e] = v[e].y;
           }
-        } else if constexpr (UNIT == 2) {
+        } else if constexpr (RU == 2) {
           float* pz = p.out.re + base;
           if ((reinterpret_cast<uintptr_t>(pz) & 7) == 0) {
             float2* pp = reinterpret_cast<float2*>(pz) + t;
@@ -1083,10 +1095,16 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
           const long long S = (long long)T * p.out.es;
           float* pr = p.out.re + base + (long long)t * p.out.es;
           float* pi = p.out.im + base + (long long)t * p.out.es;
+          if ((CPAIRS & 2) && !(reinterpret_cast<uintptr_t>(pr) & 7)) {
+            float2* pz = reinterpret_cast<float2*>(pr);   // output pairs (UNIT bit 1): 8-byte stores
 #pragma unroll
-          for (int e = 0; e < E; e++) {
-            pr[e * S] = v[e].x;
-            pi[e * S] = v[e].y;
+            for (int e = 0; e < E; e++) pz[e * (S >> 1)] = v[e];
+          } else {
+#pragma unroll
+            for (int e = 0; e < E; e++) {
+              pr[e * S] = v[e].x;
+              pi[e * S] = v[e].y;
+            }
           }
         }
       }

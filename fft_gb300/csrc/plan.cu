@@ -382,6 +382,12 @@ struct Builder {
     // interleaved pairs (im right after re in the same array) with unit pair strides
     auto pairs = [](const IOSpec& v) { return v.es == 2 && v.re.buf == v.im.buf && v.im.off == v.re.off + 1; };
     const bool iunit = !f64 && !cols && !tstore && kind == LK_C2C && !tc && pairs(in) && pairs(out);
+    // cols c2c on interleaved pairs (im right after re, every stride even,
+    // so a line's pairs are 8-byte aligned when its array is): 8-byte accesses
+    auto cpair = [](const IOSpec& v) {
+      return v.re.buf == v.im.buf && v.im.off == v.re.off + 1 && v.es % 2 == 0 && v.lo % 2 == 0 && v.hi % 2 == 0;
+    };
+    const int cpairs = (!f64 && cols && kind == LK_C2C && !tc) ? (cpair(in) ? 1 : 0) | (cpair(out) ? 2 : 0) : 0;
     if (f64) {
       if (!get_line_kernel64(logl, cols, kind, tstore, &op.k)) {
         fail("no FP64 kernel for this line length");
@@ -391,6 +397,8 @@ struct Builder {
       // same kernel with compile-time element offsets
     } else if (iunit && get_rows_c2c_iunit(logl, &op.k)) {
       // the same on interleaved pairs
+    } else if (cpairs && get_cols_c2c_pairs(logl, tstore, cpairs, &op.k)) {
+      // cols passes over interleaved pairs
     } else if (!tc && !get_line_kernel(logl, cols, kind, tstore, &op.k)) {
       fail("no kernel for this line length");
       return;
@@ -779,10 +787,11 @@ std::string describe_plan(const Plan& P) {
     if (op.type == OP_LINE) {
       snprintf(buf, sizeof buf,
                "{\"type\":\"line\",\"logl\":%d,\"cols\":%d,\"lk\":%d,\"tstore\":%d,\"tc\":%d,\"C\":%d,"
-               "\"halves\":%d,"
+               "\"halves\":%d,\"unit\":%d,"
                "\"threads\":%d,\"smem\":%zu,\"grid\":%lld,\"nlines\":%lld,\"inverse\":%d,"
                "\"tw_n\":%lld,\"tw_qmask\":%lld,\"tw_qshift\":%d,\"real_L\":%lld,\"pcols\":%lld,",
-               op.k.logl, op.k.cols, op.k.kind, op.k.tstore, op.k.tc, op.k.lines_per_cta, op.k.halves, op.threads,
+               op.k.logl, op.k.cols, op.k.kind, op.k.tstore, op.k.tc, op.k.lines_per_cta, op.k.halves, op.k.unit,
+               op.threads,
                op.smem,
                op.grid, op.p.nlines, op.p.inverse, op.p.tw_n, op.p.tw_qmask, op.p.tw_qshift, op.real_L, op.p.pcols);
     } else if (op.type == OP_REAL) {

@@ -130,3 +130,16 @@ def test_uneven_io_regions_layout():
     assert spans[-1][1] <= buf.numel()
     # the same transforms and descriptors as the interleaved layout
     assert len(U.descs(items, buf, offs)) == len(items)
+
+
+def test_cols_pair_kernels_where_pairs_are():
+    # cols passes over interleaved pairs (the real transforms' interleaved
+    # views, the interleaved format) take the 8-byte-pair kernels; split
+    # data keeps the plain ones
+    units = lambda k, d, b, f=G.afft_split: [(o["cols"], o["tstore"], o["unit"]) for o in describe(k, d, b, f)["ops"]
+                                            if o["type"] == "line"]
+    assert units("r", [1 << 20], 4)[0] == (1, 1, 1)                       # pass A reads the real pairs
+    assert units("ri", [1 << 21], 4)[-1] == (1, 0, 2)                     # pass B writes them
+    assert units("c", [65536], 4, G.afft_interleaved) == [(1, 1, 1), (1, 0, 2)]
+    assert units("c", [256, 256, 256], 1, G.afft_interleaved)[1:] == [(1, 0, 3), (1, 0, 3)]
+    assert all(u == 0 for c, _, u in units("c", [65536], 4) + units("c", [64, 64, 64], 1) if c)
