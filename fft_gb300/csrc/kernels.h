@@ -38,6 +38,10 @@ bool get_rows_c2c_iunit(int logl, LineKernel* out);
 // pairs bit 0 = input, bit 1 = output (the kernels' UNIT in cols mode), for
 // lines of 2^5 .. 2^11 points; the transposing store only with pairs = 1
 bool get_cols_c2c_pairs(int logl, bool tstore, int pairs, LineKernel* out);
+// rows C2R (lines of 2^8 .. 2^14 points) and R2C (2^12 .. 2^14) whose real
+// side (C2R output, R2C input) is written / read as pairs with unit pair
+// stride (float2 accesses)
+bool get_rows_real_pairs(int logl, int kind, LineKernel* out);
 
 // FP64 kernels (line_fft64.cuh, k_f64_*.cu): rows {C2C, R2C, C2R} up to
 // 2^13 points, cols {C2C (also with the transposing store), R2C, C2R} up to

@@ -847,8 +847,9 @@ __device__ __forceinline__ void rows_stage_out_reals(const LineParams& p, long l
 // The body of one CTA's work: lines [cta*C, cta*C + C) of the launch `p`.
 // UNIT, rows mode: 1 both element strides are 1 (split complex rows), 2 both
 // are 2 with im = re + 1 (interleaved complex rows, loaded and stored as
-// float2), so element offsets are compile-time constants instead of runtime
-// 64-bit products.  Cols mode: bit 0 the input, bit 1 the output are
+// float2; for the real kinds the real side: R2C's input, C2R's output), so
+// element offsets are compile-time constants instead of runtime 64-bit
+// products.  Cols mode: bit 0 the input, bit 1 the output are
 // interleaved pairs (im = re + 1, even strides), accessed as float2.
 template <int LOGL, int C, bool COLS, int KIND, bool TSTORE, bool TC = false, int UNIT = 0>
 __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta, TcState* ts = nullptr) {
@@ -1121,13 +1122,29 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
     }
     if (!staged_out && active) {
       const long long base = line_off(p.out, q);
-      const long long S = (long long)T * p.out.es;
-      float* pr = p.out.re + base + (long long)t * p.out.es;
-      float* pi = p.out.im + base + (long long)t * p.out.es;
+      if constexpr (RU == 2) {
+        // the real output as pairs (x[2i], x[2i+1]) with unit pair stride
+        float* pz = p.out.re + base;
+        if (!(reinterpret_cast<uintptr_t>(pz) & 7)) {
+          float2* pp = reinterpret_cast<float2*>(pz) + t;
 #pragma unroll
-      for (int e = 0; e < E; e++) {
-        pr[e * S] = v[e].x;
-        pi[e * S] = v[e].y;
+          for (int e = 0; e < E; e++) pp[T * e] = v[e];
+        } else {
+#pragma unroll
+          for (int e = 0; e < E; e++) {
+            pz[2 * (t + T * e)] = v[e].x;
+            pz[2 * (t + T * e) + 1] = v[e].y;
+          }
+        }
+      } else {
+        const long long S = (long long)T * p.out.es;
+        float* pr = p.out.re + base + (long long)t * p.out.es;
+        float* pi = p.out.im + base + (long long)t * p.out.es;
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+          pr[e * S] = v[e].x;
+          pi[e * S] = v[e].y;
+        }
       }
     }
   } else {

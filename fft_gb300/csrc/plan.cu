@@ -388,6 +388,11 @@ struct Builder {
       return v.re.buf == v.im.buf && v.im.off == v.re.off + 1 && v.es % 2 == 0 && v.lo % 2 == 0 && v.hi % 2 == 0;
     };
     const int cpairs = (!f64 && cols && kind == LK_C2C && !tc) ? (cpair(in) ? 1 : 0) | (cpair(out) ? 2 : 0) : 0;
+    // rows real kernels whose real side is pairs with unit pair stride: every
+    // C2R of 256 points and more (4-8% faster); R2C only from 4096 points
+    // (shorter R2C pair variants spill and measured 0-6% slower)
+    const bool rpairs = !f64 && !cols && !tstore &&
+                        ((kind == LK_R2C && pairs(in) && logl >= 12) || (kind == LK_C2R && pairs(out)));
     if (f64) {
       if (!get_line_kernel64(logl, cols, kind, tstore, &op.k)) {
         fail("no FP64 kernel for this line length");
@@ -399,6 +404,8 @@ struct Builder {
       // the same on interleaved pairs
     } else if (cpairs && get_cols_c2c_pairs(logl, tstore, cpairs, &op.k)) {
       // cols passes over interleaved pairs
+    } else if (rpairs && get_rows_real_pairs(logl, kind, &op.k)) {
+      // rows real passes with float2 accesses on the real side
     } else if (!tc && !get_line_kernel(logl, cols, kind, tstore, &op.k)) {
       fail("no kernel for this line length");
       return;

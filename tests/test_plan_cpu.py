@@ -143,3 +143,18 @@ def test_cols_pair_kernels_where_pairs_are():
     assert units("c", [65536], 4, G.afft_interleaved) == [(1, 1, 1), (1, 0, 2)]
     assert units("c", [256, 256, 256], 1, G.afft_interleaved)[1:] == [(1, 0, 3), (1, 0, 3)]
     assert all(u == 0 for c, _, u in units("c", [65536], 4) + units("c", [64, 64, 64], 1) if c)
+
+
+def test_rows_real_pair_kernels():
+    # rows C2R passes of 256 points and more write the real side as float2
+    # pairs, rows R2C passes of 4096 points and more read it so; shorter
+    # lines keep the strided or warp-staged accesses
+    rows = lambda k, d, b: [(o["logl"], o["lk"], o["unit"]) for o in describe(k, d, b)["ops"]
+                            if o["type"] == "line" and not o["cols"]]
+    assert rows("r", [8192], 64) == [(12, 1, 2)]
+    assert rows("ri", [1 << 15], 4) == [(14, 2, 2)]
+    assert rows("r", [256], 64) == [(7, 1, 0)]
+    assert rows("r", [4096], 64) == [(11, 1, 0)]
+    assert rows("ri", [512], 8) == [(8, 2, 2)]
+    assert rows("ri", [256], 8) == [(7, 2, 0)]
+    assert all(u != 2 for _, _, u in rows("r", [4096, 4096], 1))        # N-D rows are complex
