@@ -95,7 +95,6 @@ constexpr int lines_per_cta_k() {
 template <int LOGL, bool COLS, int KIND, bool TSTORE, bool TC = false, int UNIT = 0>
 LineKernel make_line_kernel() {
   constexpr int C = lines_per_cta_k<LOGL, COLS, KIND>();
-  constexpr int L = 1 << LOGL;
   static_assert(!TC || (size_t)LineSmem<LOGL, C, COLS, TSTORE, TC>::FLOAT2S * 8 >= (size_t)(Sched<LOGL>::T * C / 128) * 16384,
                 "TC operand tiles must fit in the exchange buffer");
   LineKernel k;

@@ -1324,14 +1324,14 @@ line_fft_grouped(const Segment* __restrict__ segs, const int* __restrict__ seg_o
       line_fft_body<LOGL, C, COLS, KIND, TSTORE, true, UNIT>(sp, v - segs[sg].cta0, &S);
     }
     tc_teardown<Sched<LOGL>::T * C>(S);
-    return;
-  }
-  for (long long v = blockIdx.x; v < total; v += gridDim.x) {
-    const int sg = __ldg(seg_of + v);
-    __syncthreads();   // a previous iteration is done with sp and the staging buffers
-    stage_params(sp, segs[sg].p);
-    __syncthreads();
-    line_fft_body<LOGL, C, COLS, KIND, TSTORE, false, UNIT>(sp, v - segs[sg].cta0);
+  } else {
+    for (long long v = blockIdx.x; v < total; v += gridDim.x) {
+      const int sg = __ldg(seg_of + v);
+      __syncthreads();   // a previous iteration is done with sp and the staging buffers
+      stage_params(sp, segs[sg].p);
+      __syncthreads();
+      line_fft_body<LOGL, C, COLS, KIND, TSTORE, false, UNIT>(sp, v - segs[sg].cta0);
+    }
   }
 }
 

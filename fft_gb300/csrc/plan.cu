@@ -496,7 +496,6 @@ struct Builder {
     op.type = OP_REAL1;
     op.rp.nlines = count;
     op.rp.inverse = forward ? 0 : 1;
-    View v;
     if (forward) {
       op.in = io(split_view(B_SRC_RE, B_SRC_RE), 1, 0, 1, 0, 0);
       op.out = io(P.format == 1 ? inter_view(B_DST_RE) : split_view(B_DST_RE, B_DST_IM), 1, 0, 1, 0, 0);
@@ -504,7 +503,6 @@ struct Builder {
       op.in = io(P.format == 1 ? inter_view(B_SRC_RE) : split_view(B_SRC_RE, B_SRC_IM), 1, 0, 1, 0, 0);
       op.out = io(split_view(B_DST_RE, B_DST_RE), 1, 0, 1, 0, 0);
     }
-    (void)v;
     op.threads = 256;
     op.grid = (count + 255) / 256;
     P.ops.push_back(op);
