@@ -690,10 +690,10 @@ std::unique_ptr<Plan> build_plan(int kind, int ndim, const long long* dims, long
         b.line(LK_C2C, true, false, l2, io(S, L1, 1, L, l1, L1 - 1), io(realv, L1, 1, L, l1, L1 - 1),
                batch * L1, true);
       } else {
-        // real pre-pass into scratch (Z'), then the inverse four-step from
+        // real pre-pass into scratch (Z', as re,im pairs so that pass A
+        // takes its 8-byte-pair loads), then the inverse four-step from
         // there into dst's interleaved view, its own scratch above Z'
-        View S = split_view(B_SCR, B_SCR, 0);
-        S.im.off = batch * L;
+        View S = inter_view(B_SCR, 0);
         b.need_scratch(2 * batch * L);
         b.real_pass(io(src, 1, 0, L + 1, 0, 0), io(S, 1, 0, L, 0, 0), batch, L, true, false);
         b.scr_base = 2 * batch * L;
