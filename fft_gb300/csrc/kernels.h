@@ -16,8 +16,8 @@ struct LineKernel {
   int kind;            // LK_C2C / LK_R2C / LK_C2R
   int tstore;          // store with the along-line mapping (four-step pass A)
   int tc;              // split-precision tensor-core butterflies
-  int unit;            // rows c2c: unit element strides, 1 split, 2 interleaved; cols c2c:
-                       // interleaved pairs, bit 0 input, bit 1 output
+  int unit;            // rows: unit element strides, 1 split, 2 pairs (c2c interleaved, or the
+                       // real side of R2C / C2R); cols: pairs, bit 0 input, bit 1 output
   int lines_per_cta;   // C
   int threads;         // T * C
   size_t smem;         // bytes of dynamic shared memory
@@ -36,8 +36,11 @@ bool get_rows_c2c_unit(int logl, bool tc, LineKernel* out);
 bool get_rows_c2c_iunit(int logl, LineKernel* out);
 // cols c2c on interleaved pairs (im right after re, even element stride):
 // pairs bit 0 = input, bit 1 = output (the kernels' UNIT in cols mode), for
-// lines of 2^5 .. 2^11 points; the transposing store only with pairs = 1
+// lines of 2^5 .. 2^11 points; the transposing store with pairs 1 or 3
 bool get_cols_c2c_pairs(int logl, bool tstore, int pairs, LineKernel* out);
+// the paired R2C pass (four-step pass B of a long 1D real forward) with its
+// input as float2 pairs, lines of 2^7 .. 2^11 points
+bool get_r2c_paired_pairs(int logl, LineKernel* out);
 // rows C2R (lines of 2^8 .. 2^14 points) and R2C (2^12 .. 2^14) whose real
 // side (C2R output, R2C input) is written / read as pairs with unit pair
 // stride (float2 accesses)

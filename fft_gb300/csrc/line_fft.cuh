@@ -481,7 +481,7 @@ __device__ __forceinline__ long long paired_column(int c, long long a, long long
 // (k = k1 + L1 k2, written where the unfused pass B would write Z[k]), and
 // the column-0 thread of k2 = 0 also writes X[L] (element L2 of line
 // (o, 0)).  Lines come in whole tiles: L1 is a multiple of C.
-template <int LOGL, int C>
+template <int LOGL, int C, bool PIN = false>
 __device__ __forceinline__ void r2c_paired_body(const LineParams& p, long long cta) {
   using Sc = Sched<LOGL>;
   constexpr int L2 = Sc::L, E = Sc::E, T = Sc::T, H = C / 2;
@@ -503,8 +503,20 @@ __device__ __forceinline__ void r2c_paired_body(const LineParams& p, long long c
     const long long S = (long long)T * p.in.es;
     const float* pr = p.in.re + base + (long long)t * p.in.es;
     const float* pi = p.in.im + base + (long long)t * p.in.es;
+    bool loaded = false;
+    if constexpr (PIN) {
+      // input pairs (im = re + 1, even element stride): 8-byte loads
+      if (!(reinterpret_cast<uintptr_t>(pr) & 7)) {
+        const float2* pz = reinterpret_cast<const float2*>(pr);
 #pragma unroll
-    for (int e = 0; e < E; e++) v[e] = make_float2(__ldg(pr + e * S), __ldg(pi + e * S));
+        for (int e = 0; e < E; e++) v[e] = __ldg(pz + e * (S >> 1));
+        loaded = true;
+      }
+    }
+    if (!loaded) {
+#pragma unroll
+      for (int e = 0; e < E; e++) v[e] = make_float2(__ldg(pr + e * S), __ldg(pi + e * S));
+    }
   }
   run_stages<LOGL, C, true, false, 0>(v, t, c, p.tw, sm);
 
@@ -850,7 +862,8 @@ __device__ __forceinline__ void rows_stage_out_reals(const LineParams& p, long l
 // float2; for the real kinds the real side: R2C's input, C2R's output), so
 // element offsets are compile-time constants instead of runtime 64-bit
 // products.  Cols mode: bit 0 the input, bit 1 the output are
-// interleaved pairs (im = re + 1, even strides), accessed as float2.
+// interleaved pairs (im = re + 1, even strides), accessed as float2 (the
+// paired R2C pass: bit 0 only).
 template <int LOGL, int C, bool COLS, int KIND, bool TSTORE, bool TC = false, int UNIT = 0>
 __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta, TcState* ts = nullptr) {
   if constexpr (KIND == LK_R2C_HALF) {
@@ -860,7 +873,7 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
   }
   if constexpr (KIND == LK_R2C_PAIRED) {
     static_assert(COLS && !TSTORE && !TC, "the paired R2C pass is a plain cols pass");
-    r2c_paired_body<LOGL, C>(p, cta);
+    r2c_paired_body<LOGL, C, (UNIT & 1) != 0>(p, cta);
     return;
   }
   if constexpr (KIND == LK_C2R_PAIRED) {
@@ -1038,8 +1051,34 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
           else if (p.tw_full) emit(std::integral_constant<int, 1>{}, unit);
           else emit(std::integral_constant<int, 2>{}, unit);
         };
-        if (p.out.es == 1) emit_tw(std::true_type{});
-        else emit_tw(std::false_type{});
+        bool stored = false;
+        if constexpr ((CPAIRS & 2) != 0) {
+          // output pairs (im = re + 1, element stride 2): one 8-byte store
+          // per element
+          float* pz = p.out.re + base + 2LL * t2;
+          if (p.out.es == 2 && !(reinterpret_cast<uintptr_t>(pz) & 7)) {
+            float2* pp = reinterpret_cast<float2*>(pz);
+            auto emit2 = [&](auto tw) {
+              constexpr int TW = decltype(tw)::value;
+#pragma unroll
+              for (int e = 0; e < E; e++) {
+                float2 x = sm.get(c2, t2 + T * e);
+                if constexpr (TW) x = cmul(x, fourstep_twiddle<L, TW == 1>(p, q2, t2 + T * e));
+                pp[T * e] = inv ? cswap(x) : x;
+              }
+            };
+            if (!p.tw_n) emit2(std::integral_constant<int, 0>{});
+            else if (p.tw_full) emit2(std::integral_constant<int, 1>{});
+            else emit2(std::integral_constant<int, 2>{});
+            stored = true;
+          }
+        }
+        if (stored) {
+        } else if (p.out.es == 1) {
+          emit_tw(std::true_type{});
+        } else {
+          emit_tw(std::false_type{});
+        }
       }
     } else {
       // four-step twiddles only occur in cols passes

@@ -404,6 +404,8 @@ struct Builder {
       // the same on interleaved pairs
     } else if (cpairs && get_cols_c2c_pairs(logl, tstore, cpairs, &op.k)) {
       // cols passes over interleaved pairs
+    } else if (!f64 && kind == LK_R2C_PAIRED && cpair(in) && get_r2c_paired_pairs(logl, &op.k)) {
+      // the paired R2C pass over pairs
     } else if (rpairs && get_rows_real_pairs(logl, kind, &op.k)) {
       // rows real passes with float2 accesses on the real side
     } else if (!tc && !get_line_kernel(logl, cols, kind, tstore, &op.k)) {
@@ -646,11 +648,11 @@ std::unique_ptr<Plan> build_plan(int kind, int ndim, const long long* dims, long
     } else if (kind == K_R) {
       // four-step pass A (twiddle, transposing store) into scratch, then
       // pass B over mirrored column pairs with the real post-pass fused,
-      // into dst lines of L + 1 bins
+      // into dst lines of L + 1 bins; the scratch holds re,im pairs (8-byte
+      // accesses on both sides)
       const int logl = ilog2ll(L), l1 = b.l1_of(logl), l2 = logl - l1;
       const long long L1 = 1LL << l1, L2 = 1LL << l2;
-      View S = split_view(B_SCR, B_SCR, 0);
-      S.im.off = batch * L;
+      View S = inter_view(B_SCR, 0);
       b.need_scratch(2 * batch * L);
       b.line(LK_C2C, true, true, l1, io(realv, L2, 1, L, l2, L2 - 1), io(S, 1, L1, L, l2, L2 - 1), batch * L2,
              false, L, L2 - 1, 0);

@@ -138,7 +138,7 @@ def test_cols_pair_kernels_where_pairs_are():
     # data keeps the plain ones
     units = lambda k, d, b, f=G.afft_split: [(o["cols"], o["tstore"], o["unit"]) for o in describe(k, d, b, f)["ops"]
                                             if o["type"] == "line"]
-    assert units("r", [1 << 20], 4)[0] == (1, 1, 1)                       # pass A reads the real pairs
+    assert units("r", [1 << 20], 4) == [(1, 1, 3), (1, 0, 1)]             # pairs: real input, scratch, scratch
     assert units("ri", [1 << 21], 4)[-1] == (1, 0, 2)                     # pass B writes them
     assert units("c", [65536], 4, G.afft_interleaved) == [(1, 1, 1), (1, 0, 2)]
     assert units("c", [256, 256, 256], 1, G.afft_interleaved)[1:] == [(1, 0, 3), (1, 0, 3)]
