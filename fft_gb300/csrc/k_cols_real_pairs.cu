@@ -1,5 +1,6 @@
 // four-step pass B of a long 1D real forward transform (the paired R2C pass)
-// reading its input as float2 pairs, L = 2^7 .. 2^11
+// reading its input as float2 pairs, L = 2^7 .. 2^11; pass A of a long 1D
+// real inverse (the paired C2R pass) writing its output so, L = 2^7 .. 2^9
 #include "kernels.h"
 
 namespace agb {
@@ -11,6 +12,15 @@ bool get_r2c_paired_pairs(int logl, LineKernel* out) {
     case 9: *out = make_line_kernel<9, true, LK_R2C_PAIRED, false, false, 1>(); return true;
     case 10: *out = make_line_kernel<10, true, LK_R2C_PAIRED, false, false, 1>(); return true;
     case 11: *out = make_line_kernel<11, true, LK_R2C_PAIRED, false, false, 1>(); return true;
+    default: return false;
+  }
+}
+
+bool get_c2r_paired_pairs(int logl, LineKernel* out) {
+  switch (logl) {
+    case 7: *out = make_line_kernel<7, true, LK_C2R_PAIRED, true, false, 2>(); return true;
+    case 8: *out = make_line_kernel<8, true, LK_C2R_PAIRED, true, false, 2>(); return true;
+    case 9: *out = make_line_kernel<9, true, LK_C2R_PAIRED, true, false, 2>(); return true;
     default: return false;
   }
 }

@@ -41,6 +41,9 @@ bool get_cols_c2c_pairs(int logl, bool tstore, int pairs, LineKernel* out);
 // the paired R2C pass (four-step pass B of a long 1D real forward) with its
 // input as float2 pairs, lines of 2^7 .. 2^11 points
 bool get_r2c_paired_pairs(int logl, LineKernel* out);
+// the paired C2R pass (four-step pass A of a long 1D real inverse) with its
+// output as float2 pairs, lines of 2^7 .. 2^9 points
+bool get_c2r_paired_pairs(int logl, LineKernel* out);
 // rows C2R (lines of 2^8 .. 2^14 points) and R2C (2^12 .. 2^14) whose real
 // side (C2R output, R2C input) is written / read as pairs with unit pair
 // stride (float2 accesses)

@@ -560,7 +560,7 @@ __device__ __forceinline__ void r2c_paired_body(const LineParams& p, long long c
 // reads inside one CTA, so the second hits the cache.  Then the ordinary pass
 // A work: inverse (re/im swapped) stages, the four-step twiddle and the
 // transposing store, all with the paired line mapping.
-template <int LOGL, int C>
+template <int LOGL, int C, bool POUT = false>
 __device__ __forceinline__ void c2r_paired_body(const LineParams& p, long long cta) {
   using Sc = Sched<LOGL>;
   constexpr int L1 = Sc::L, E = Sc::E, T = Sc::T;
@@ -612,6 +612,23 @@ __device__ __forceinline__ void c2r_paired_body(const LineParams& p, long long c
   const long long SO = (long long)T * p.out.es;
   float* por = p.out.re + base + (long long)tt * p.out.es;
   float* poi = p.out.im + base + (long long)tt * p.out.es;
+  if constexpr (POUT) {
+    // output pairs (im = re + 1, element stride 2): 8-byte stores
+    float* pz = p.out.re + base + 2LL * tt;
+    if (p.out.es == 2 && !(reinterpret_cast<uintptr_t>(pz) & 7)) {
+      float2* pp = reinterpret_cast<float2*>(pz);
+      auto emit2 = [&](auto full) {
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+          const int k1 = tt + T * e;
+          pp[T * e] = cswap(cmul(sm.get(c2, k1), fourstep_twiddle<L1, decltype(full)::value>(p, q2, k1)));
+        }
+      };
+      if (p.tw_full) emit2(std::true_type{});
+      else emit2(std::false_type{});
+      return;
+    }
+  }
   auto emit = [&](auto full) {
 #pragma unroll
     for (int e = 0; e < E; e++) {
@@ -863,7 +880,7 @@ __device__ __forceinline__ void rows_stage_out_reals(const LineParams& p, long l
 // element offsets are compile-time constants instead of runtime 64-bit
 // products.  Cols mode: bit 0 the input, bit 1 the output are
 // interleaved pairs (im = re + 1, even strides), accessed as float2 (the
-// paired R2C pass: bit 0 only).
+// paired R2C pass: bit 0 only; the paired C2R pass: bit 1 only).
 template <int LOGL, int C, bool COLS, int KIND, bool TSTORE, bool TC = false, int UNIT = 0>
 __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta, TcState* ts = nullptr) {
   if constexpr (KIND == LK_R2C_HALF) {
@@ -878,7 +895,7 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
   }
   if constexpr (KIND == LK_C2R_PAIRED) {
     static_assert(COLS && TSTORE && !TC, "the paired C2R pass is pass A of a four-step");
-    c2r_paired_body<LOGL, C>(p, cta);
+    c2r_paired_body<LOGL, C, (UNIT & 2) != 0>(p, cta);
     return;
   }
   using Sc = Sched<LOGL>;

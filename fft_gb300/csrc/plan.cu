@@ -406,6 +406,8 @@ struct Builder {
       // cols passes over interleaved pairs
     } else if (!f64 && kind == LK_R2C_PAIRED && cpair(in) && get_r2c_paired_pairs(logl, &op.k)) {
       // the paired R2C pass over pairs
+    } else if (!f64 && kind == LK_C2R_PAIRED && cpair(out) && get_c2r_paired_pairs(logl, &op.k)) {
+      // the paired C2R pass into pairs
     } else if (rpairs && get_rows_real_pairs(logl, kind, &op.k)) {
       // rows real passes with float2 accesses on the real side
     } else if (!tc && !get_line_kernel(logl, cols, kind, tstore, &op.k)) {
@@ -679,8 +681,7 @@ std::unique_ptr<Plan> build_plan(int kind, int ndim, const long long* dims, long
         // faster on GB300 (64 x 2^20: 0.369 vs 0.384 ms)
         const int l1 = l1p, l2 = logl - l1;
         const long long L1 = 1LL << l1, L2 = 1LL << l2;
-        View S = split_view(B_SCR, B_SCR, 0);
-        S.im.off = batch * L;
+        View S = inter_view(B_SCR, 0);   // re,im pairs: 8-byte accesses on both sides
         b.need_scratch(2 * batch * L);
         b.line(LK_C2R_PAIRED, true, true, l1, io(src, L2, 1, L + 1, l2, L2 - 1), io(S, 1, L1, L, l2, L2 - 1),
                batch * L2, true, L, L2 - 1, 0, L);
