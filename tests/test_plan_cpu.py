@@ -158,3 +158,24 @@ def test_rows_real_pair_kernels():
     assert rows("ri", [512], 8) == [(8, 2, 2)]
     assert rows("ri", [256], 8) == [(7, 2, 0)]
     assert all(u != 2 for _, _, u in rows("r", [4096, 4096], 1))        # N-D rows are complex
+
+
+def test_long_real_scratch_is_pairs():
+    # the long 1D real transforms keep their four-step scratch (and the long
+    # inverse's standalone Z') as re,im pairs: every access on both sides of
+    # it is an 8-byte pair, and the scratch size is unchanged
+    def ops(k, d, b):
+        return [(o["type"], o.get("cols"), o.get("tstore"), o.get("lk"), o.get("unit"))
+                for o in describe(k, d, b)["ops"]]
+    assert ops("r", [1 << 19], 8) == [("line", 1, 1, 0, 3), ("line", 1, 0, 4, 1)]
+    assert ops("ri", [1 << 19], 8) == [("line", 1, 1, 5, 2), ("line", 1, 0, 0, 3)]
+    assert ops("ri", [1 << 21], 2) == [("real", None, None, None, None), ("line", 1, 1, 0, 1),
+                                      ("line", 1, 0, 0, 2)]
+    for k, d, b in (("r", [1 << 19], 8), ("ri", [1 << 19], 8)):
+        plan = describe(k, d, b)
+        s = [o for o in plan["ops"] if o["type"] == "line"]
+        scr = s[0]["out"]                                   # pass A's output, pass B's input
+        assert scr["re"][0] == scr["im"][0] and scr["im"][1] == scr["re"][1] + 1 and scr["es"] == 2
+        assert plan["scratch_elems"] >= 2 * b * (d[0] // 2)
+    d = describe("ri", [1 << 21], 2)["ops"][0]["out"]       # Z' of the standalone pre-pass
+    assert d["im"][1] == d["re"][1] + 1 and d["es"] == 2
