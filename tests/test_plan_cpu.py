@@ -9,7 +9,7 @@ import fft_gb300 as G
 from oracle import oracle as O
 from plan_emulator import describe, run
 
-SHAPES = [[1], [2], [4], [16], [32], [256], [4096], [16384], [32768], [1 << 16], [1 << 19],
+SHAPES = [[1], [2], [4], [16], [32], [256], [4096], [16384], [32768], [1 << 16], [1 << 19], [1 << 20], [1 << 21],
           [2, 2], [4, 8], [64, 4], [8, 4096], [4096, 8], [16, 2048, 2], [8192, 4], [2, 16384],
           [2, 4, 8], [16, 16, 16], [4, 4, 4, 4], [2, 2, 2, 2, 2], [1, 32, 1], [4, 1, 1, 8]]
 
