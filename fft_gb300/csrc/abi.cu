@@ -395,38 +395,64 @@ static int transform_sync(void* plan, const float* sr, const float* si, float* d
       P->chunk = build_plan(P->kind, P->ndim, P->dims, P->batch / k, P->format, false, P->form);
       if (!P->chunk) k = 1;
     }
-    P->nchunks = k;
-    if (cudaStreamCreateWithFlags(&P->copy_in, cudaStreamDefault) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&P->copy_out, cudaStreamDefault) != cudaSuccess) {
+    // streams and events are set up all or nothing: copy_in, set last,
+    // marks them ready
+    cudaStream_t s_in = nullptr, s_out = nullptr;
+    std::vector<cudaEvent_t> ev(2 * k, nullptr);
+    bool ok = cudaStreamCreateWithFlags(&s_in, cudaStreamDefault) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&s_out, cudaStreamDefault) == cudaSuccess;
+    for (auto& e : ev) ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
       cudaGetLastError();
-      set_error(AFFT_GB300_ECUDA, "stream creation failed");
+      for (auto e : ev)
+        if (e) cudaEventDestroy(e);
+      if (s_in) cudaStreamDestroy(s_in);
+      if (s_out) cudaStreamDestroy(s_out);
+      set_error(AFFT_GB300_ECUDA, "stream or event creation failed");
       return AFFT_GB300_ECUDA;
     }
-    P->ev.resize(2 * k);
-    for (auto& e : P->ev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    P->nchunks = k;
+    P->ev = std::move(ev);
+    P->copy_out = s_out;
+    P->copy_in = s_in;
   }
   const long long k = P->nchunks;
   const size_t cin = fin / k, cout = fout / k;    // bytes per chunk, per array
   auto f = [](char* p) { return reinterpret_cast<float*>(p); };
+  // the first error of any enqueue call (a rejected copy is reported by the
+  // call itself, not by a later synchronize)
+  cudaError_t ce = cudaSuccess;
+  auto chk = [&ce](cudaError_t r) {
+    if (ce == cudaSuccess) ce = r;
+  };
   for (long long i = 0; i < k; i++) {
-    cudaMemcpyAsync(d_sr + i * cin, h_sr + i * cin, cin, cudaMemcpyDefault, P->copy_in);
-    if (use_si) cudaMemcpyAsync(d_si + i * cin, h_si + i * cin, cin, cudaMemcpyDefault, P->copy_in);
-    cudaEventRecord(P->ev[2 * i], P->copy_in);
+    chk(cudaMemcpyAsync(d_sr + i * cin, h_sr + i * cin, cin, cudaMemcpyDefault, P->copy_in));
+    if (use_si) chk(cudaMemcpyAsync(d_si + i * cin, h_si + i * cin, cin, cudaMemcpyDefault, P->copy_in));
+    chk(cudaEventRecord(P->ev[2 * i], P->copy_in));
   }
   Plan& C = k > 1 ? *P->chunk : *P;
+  int rc = 0;
   for (long long i = 0; i < k; i++) {
-    cudaStreamWaitEvent(P->stream, P->ev[2 * i], 0);
-    int rc = C.launch(f(d_sr + i * cin), use_si ? f(d_si + i * cin) : nullptr, f(d_dr + i * cout),
-                      use_di ? f(d_di + i * cout) : nullptr, P->stream);
-    if (rc) return rc;
-    cudaEventRecord(P->ev[2 * i + 1], P->stream);
-    cudaStreamWaitEvent(P->copy_out, P->ev[2 * i + 1], 0);
-    cudaMemcpyAsync(h_dr + i * cout, d_dr + i * cout, cout, cudaMemcpyDefault, P->copy_out);
-    if (use_di) cudaMemcpyAsync(h_di + i * cout, d_di + i * cout, cout, cudaMemcpyDefault, P->copy_out);
+    chk(cudaStreamWaitEvent(P->stream, P->ev[2 * i], 0));
+    rc = C.launch(f(d_sr + i * cin), use_si ? f(d_si + i * cin) : nullptr, f(d_dr + i * cout),
+                  use_di ? f(d_di + i * cout) : nullptr, P->stream);
+    if (rc) break;
+    chk(cudaEventRecord(P->ev[2 * i + 1], P->stream));
+    chk(cudaStreamWaitEvent(P->copy_out, P->ev[2 * i + 1], 0));
+    chk(cudaMemcpyAsync(h_dr + i * cout, d_dr + i * cout, cout, cudaMemcpyDefault, P->copy_out));
+    if (use_di) chk(cudaMemcpyAsync(h_di + i * cout, d_di + i * cout, cout, cudaMemcpyDefault, P->copy_out));
   }
-  cudaError_t e = cudaStreamSynchronize(P->copy_out);
+  // every copy from or to the caller's memory has ended when the call returns
+  cudaError_t e = cudaStreamSynchronize(P->copy_in);
   if (e == cudaSuccess) e = cudaStreamSynchronize(P->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(P->copy_out);
+  if (rc) {
+    cudaGetLastError();
+    return rc;   // the launch reported its own error
+  }
+  if (e == cudaSuccess) e = ce;
   if (e != cudaSuccess) {
+    cudaGetLastError();
     set_error(AFFT_GB300_ECUDA, cudaGetErrorString(e));
     return AFFT_GB300_ECUDA;
   }

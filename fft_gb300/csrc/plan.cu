@@ -186,8 +186,15 @@ const __half* tc_matrix_table() {
       h[1024 + nn * 32 + kk] = __double2half((m - (double)__half2float(mh)) * 2048.0);
     }
   __half* d = nullptr;
-  if (cudaMalloc(&d, 2048 * sizeof(__half)) != cudaSuccess) return nullptr;
-  cudaMemcpy(d, h.data(), 2048 * sizeof(__half), cudaMemcpyHostToDevice);
+  if (cudaMalloc(&d, 2048 * sizeof(__half)) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (cudaMemcpy(d, h.data(), 2048 * sizeof(__half), cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(d);
+    return nullptr;
+  }
   tabs[dev] = d;
   return d;
 }
@@ -201,8 +208,15 @@ int* tc_error_word() {
   auto it = words.find(dev);
   if (it != words.end()) return it->second;
   int* d = nullptr;
-  if (cudaMalloc(&d, sizeof(int)) != cudaSuccess) return nullptr;
-  cudaMemset(d, 0, sizeof(int));
+  if (cudaMalloc(&d, sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (cudaMemset(d, 0, sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(d);
+    return nullptr;
+  }
   words[dev] = d;
   return d;
 }
