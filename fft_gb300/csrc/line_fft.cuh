@@ -21,6 +21,13 @@
 // bank-conflict free.  Stage twiddles come from a per-length table computed
 // in FP64 on the host and rounded once.
 //
+// The template parameter UNIT picks compile-time access forms: in rows mode
+// unit-stride split lines (1) or re,im pairs with unit pair stride (2); in
+// cols mode re,im pairs on the input (bit 0) and/or the output (bit 1).  Pair
+// forms move one 8-byte value per element; they check 8-byte alignment at run
+// time and fall back to 4-byte accesses (callers may pass any 4-byte-aligned
+// array).
+//
 // This restates the work of afft's onedim.hpp (radix-4/8/16 passes,
 // onedim.hpp:55-507) and multi.hpp (passes along strided dims,
 // multi.hpp:18-259) as one self-sorting (Stockham) formulation, so no
