@@ -9,10 +9,8 @@ namespace agb {
 
 template <int LOGL>
 static bool cols_pairs_one(bool tstore, int pairs, LineKernel* out) {
-  if (tstore && pairs == 1) *out = make_line_kernel<LOGL, true, LK_C2C, true, false, 1>();
-  else if (tstore && pairs == 3) *out = make_line_kernel<LOGL, true, LK_C2C, true, false, 3>();
-  else if (tstore) return false;
-  else if (pairs == 1) *out = make_line_kernel<LOGL, true, LK_C2C, false, false, 1>();
+  if (tstore) return get_cols_c2c_pairs_tstore(LOGL, pairs, out);
+  if (pairs == 1) *out = make_line_kernel<LOGL, true, LK_C2C, false, false, 1>();
   else if (pairs == 2) *out = make_line_kernel<LOGL, true, LK_C2C, false, false, 2>();
   else if (pairs == 3) *out = make_line_kernel<LOGL, true, LK_C2C, false, false, 3>();
   else return false;

@@ -38,6 +38,8 @@ bool get_rows_c2c_iunit(int logl, LineKernel* out);
 // pairs bit 0 = input, bit 1 = output (the kernels' UNIT in cols mode), for
 // lines of 2^5 .. 2^11 points; the transposing store with pairs 1 or 3
 bool get_cols_c2c_pairs(int logl, bool tstore, int pairs, LineKernel* out);
+// the transposing-store half of it (k_cols_pairs_ts.cu)
+bool get_cols_c2c_pairs_tstore(int logl, int pairs, LineKernel* out);
 // the paired R2C pass (four-step pass B of a long 1D real forward) with its
 // input as float2 pairs, lines of 2^7 .. 2^11 points
 bool get_r2c_paired_pairs(int logl, LineKernel* out);
