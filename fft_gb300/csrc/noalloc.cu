@@ -86,6 +86,10 @@ static int noalloc_setup(int dev, NoallocDevice** out) {
     if (e == cudaSuccess) e = cudaGetSymbolAddress((void**)&D.stage, g_noalloc_stage);
     if (e == cudaSuccess) e = cudaGetSymbolAddress((void**)&D.hi, g_noalloc_hi);
     if (e == cudaSuccess) e = cudaGetSymbolAddress((void**)&D.lo, g_noalloc_lo);
+    // the copies above come from pageable host memory and may return before
+    // their DMA lands; the kernels run on the caller's stream, which need not
+    // order after the default stream, so wait here once
+    if (e == cudaSuccess) e = cudaStreamSynchronize(0);
     if (e != cudaSuccess) {
       cudaGetLastError();
       set_error(AFFT_GB300_ECUDA, std::string("no-alloc set-up failed: ") + cudaGetErrorString(e));
@@ -116,8 +120,9 @@ using namespace agb;
 extern "C" int afft_gb300_c2c_noalloc(const float* src_re, const float* src_im, float* dst_re, float* dst_im,
                                       size_t n, size_t batch, int inverse, void* stream) {
   clear_error();
+  // batch is compared by division: n * batch can wrap in 64 bits
   if (n < (1u << kNoallocMinLog) || n > (1u << kNoallocMaxLog) || (n & (n - 1)) || batch == 0 ||
-      (unsigned long long)n * batch > (unsigned long long)kNoallocMaxElems) {
+      batch > (size_t)kNoallocMaxElems / n) {
     set_error(AFFT_GB300_EINVAL,
               "no-alloc transform: n must be a power of two in [2^15, 2^21] and n*batch <= 2^21 "
               "(its scratch is a fixed 16 MiB device array)");
@@ -168,11 +173,13 @@ extern "C" int afft_gb300_c2c_noalloc(const float* src_re, const float* src_im, 
       return AFFT_GB300_ECUDA;
     }
     op.k.fn<<<(unsigned)op.grid, op.threads, op.smem, (cudaStream_t)stream>>>(p);
-  }
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) {
-    set_error(AFFT_GB300_ECUDA, std::string("kernel launch failed: ") + cudaGetErrorString(e));
-    return AFFT_GB300_ECUDA;
+    // stop at the first failed pass: a later pass would read stale scratch
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      set_error(AFFT_GB300_ECUDA, std::string("kernel launch failed (pass ") + std::to_string(&op - P->ops.data()) +
+                                      "): " + cudaGetErrorString(e));
+      return AFFT_GB300_ECUDA;
+    }
   }
   return 0;
 }

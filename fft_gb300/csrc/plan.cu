@@ -101,7 +101,12 @@ static auto cached_table(int type, long long key, F make) -> const typename decl
   V* d = nullptr;
   size_t bytes = std::max<size_t>(host.size(), 1) * sizeof(V);
   if (cudaMalloc(&d, bytes) != cudaSuccess) return nullptr;
-  if (!host.empty() && cudaMemcpy(d, host.data(), host.size() * sizeof(V), cudaMemcpyHostToDevice) != cudaSuccess) {
+  // a copy from pageable memory may return before its DMA lands, and plans
+  // launch on streams that need not order after the default stream: wait
+  // once, before the table is published
+  if (!host.empty() && (cudaMemcpy(d, host.data(), host.size() * sizeof(V), cudaMemcpyHostToDevice) != cudaSuccess ||
+                        cudaStreamSynchronize(0) != cudaSuccess)) {
+    cudaGetLastError();
     cudaFree(d);
     return nullptr;
   }
@@ -190,7 +195,8 @@ const __half* tc_matrix_table() {
     cudaGetLastError();
     return nullptr;
   }
-  if (cudaMemcpy(d, h.data(), 2048 * sizeof(__half), cudaMemcpyHostToDevice) != cudaSuccess) {
+  if (cudaMemcpy(d, h.data(), 2048 * sizeof(__half), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaStreamSynchronize(0) != cudaSuccess) {
     cudaGetLastError();
     cudaFree(d);
     return nullptr;
@@ -212,7 +218,7 @@ int* tc_error_word() {
     cudaGetLastError();
     return nullptr;
   }
-  if (cudaMemset(d, 0, sizeof(int)) != cudaSuccess) {
+  if (cudaMemset(d, 0, sizeof(int)) != cudaSuccess || cudaStreamSynchronize(0) != cudaSuccess) {
     cudaGetLastError();
     cudaFree(d);
     return nullptr;

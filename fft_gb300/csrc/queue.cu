@@ -228,6 +228,13 @@ static int build_queue(QueueImpl& Q) {
       return AFFT_GB300_ENOMEM;
     }
   }
+  // the uploads above come from pageable memory and may return before their
+  // DMA lands; the queue runs on the caller's stream, so wait once here
+  if (cudaStreamSynchronize(0) != cudaSuccess) {
+    cudaGetLastError();
+    set_error(AFFT_GB300_ECUDA, "queue descriptor upload failed");
+    return AFFT_GB300_ECUDA;
+  }
   std::stable_sort(Q.groups.begin(), Q.groups.end(), [](const Group& a, const Group& b) {
     return a.level != b.level ? a.level < b.level : a.total > b.total;
   });
