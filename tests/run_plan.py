@@ -1,6 +1,6 @@
 """Run one batched plan on seeded device data a few times, for profiling.
 
-    python -m fft_gb300.run_plan KIND DIMS BATCH [REPS] [FORM]
+    python tests/run_plan.py KIND DIMS BATCH [REPS] [FORM]
 
 KIND is c, ci, r or ri; DIMS a JSON list such as [256,256,256]; FORM plain
 (default), tc or f64 (double data through the FP64 kernels).  Each
@@ -8,11 +8,13 @@ repetition launches the plan's kernels once on the CUDA default stream;
 the script synchronises at the end and prints the launches per transform.
 """
 import json
+import os
 import sys
 
 import torch
 
-from . import BatchPlan
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+from fft_gb300 import BatchPlan  # noqa: E402
 
 
 def main(argv):

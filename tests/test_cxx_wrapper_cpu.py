@@ -10,7 +10,7 @@ import pytest
 import fft_gb300 as G
 from conftest import ROOT
 
-REF = "/root/reference"
+REF = os.environ.get("AFFT_REF_SRC", "/root/reference")
 HERE = os.path.join(ROOT, "tests", "cxx")
 
 

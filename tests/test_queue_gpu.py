@@ -1,4 +1,4 @@
-"""The multi-transform queue (device-side descriptor tables, one persistent
+"""The multi-transform queue (device-side descriptor tables, one grouped
 launch per (pass level, kernel shape), graph-captured) against the FP64
 oracle, transform by transform."""
 import numpy as np
