@@ -12,7 +12,10 @@ path live behind it (see afft_oracle.h for file:line citations):
 
 Also ``ref_lib()``: the reference library itself, when oracle/_ref was built
 here from the reference's sources (x86-64 only); used to pin the oracle and to
-generate the golden fixtures.
+generate the golden fixtures.  ``RefBatch`` / ``ref_mixed`` drive the
+reference library (every backend on x86-64, or its scalar backend built on
+any host from the staged sources) through its own C API over many
+transforms and host threads: the CPU baseline when it is available.
 """
 import ctypes
 import os
@@ -23,6 +26,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libafft_ref.so")
+REF_SCALAR_PATH = os.path.join(HERE, "_ref", "libafft_ref_scalar.so")
 
 C, CI, R, RI = 0, 1, 2, 3
 KINDS = {"c": C, "ci": CI, "r": R, "ri": RI}
@@ -277,3 +281,126 @@ def afft_error(y, ref):
     num = sum(float(np.sum((np.asarray(a, np.float64) - np.asarray(b, np.float64)) ** 2)) for a, b in zip(ys, rs))
     den = sum(float(np.sum(np.asarray(a, np.float64) ** 2 + np.asarray(b, np.float64) ** 2)) for a, b in zip(ys, rs))
     return (num / den) ** 0.5 if den > 0 else num ** 0.5
+
+
+_bench = {}
+
+
+def ref_bench_lib():
+    """(library, impl id, description) of the reference afft build that the
+    CPU baseline times, or None: every backend with afft_auto picking the
+    best (x86-64), else the scalar backend, the one afft builds on Arm."""
+    for path, impl, what in ((REF_PATH, 0, "afft, best SIMD backend (afft_auto)"),
+                             (REF_SCALAR_PATH, 1, "afft, scalar backend (the backend afft builds on this host)")):
+        if path in _bench:
+            if _bench[path] is not None:
+                return _bench[path]
+            continue
+        got = None
+        if os.path.exists(path):
+            try:
+                L = ctypes.CDLL(path)
+                P, I64 = ctypes.c_void_p, ctypes.c_int64
+                L.refbatch_ctx_create.restype = P
+                L.refbatch_ctx_create.argtypes = [ctypes.c_int]
+                L.refbatch_ctx_destroy.argtypes = [P]
+                L.refbatch_uniform.restype = ctypes.c_int
+                L.refbatch_uniform.argtypes = [P, ctypes.c_int, ctypes.c_size_t, P, I64, ctypes.c_int, ctypes.c_int,
+                                               P, P, P, P]
+                L.refbatch_mixed.restype = ctypes.c_int
+                L.refbatch_mixed.argtypes = [P, I64, P, P, P, P, P, P, P, ctypes.c_int, ctypes.c_int]
+                got = (L, impl, what)
+            except (OSError, AttributeError):
+                got = None
+        _bench[path] = got
+        if got is not None:
+            return got
+    return None
+
+
+class RefBatch:
+    """Dense batches of one shape through the reference afft library's C
+    API, split over host threads with one plan per thread (afft plans are
+    not reentrant).  Same call form as Port32."""
+
+    DTYPE = np.float32
+
+    def __init__(self, kind, dims, threads):
+        got = ref_bench_lib()
+        if got is None:
+            raise RuntimeError("reference afft library not built")
+        self.L, self.impl, self.what = got
+        self.kind = kind
+        self.dims = squeeze(dims)
+        self.threads = max(1, int(threads))
+        self._d = np.array(self.dims, dtype=np.uint64)
+        n = int(np.prod(self.dims, dtype=np.int64))
+        h = half_elems(self.dims)
+        self.in_elems = h if kind == "ri" else n
+        self.out_elems = h if kind == "r" else n
+        self._ctx = self.L.refbatch_ctx_create(self.threads)
+        if not self._ctx:
+            raise MemoryError("refbatch context")
+
+    def __del__(self):
+        c = getattr(self, "_ctx", None)
+        if c:
+            self.L.refbatch_ctx_destroy(c)
+            self._ctx = None
+
+    def __call__(self, a, b=None, batch=1, threads=None, out=None):
+        a = np.ascontiguousarray(a, self.DTYPE).ravel()
+        b = None if b is None else np.ascontiguousarray(b, self.DTYPE).ravel()
+        if out is None:
+            ore = np.empty(batch * self.out_elems, self.DTYPE)
+            oim = None if self.kind == "ri" else np.empty(batch * self.out_elems, self.DTYPE)
+        else:
+            ore, oim = out
+        t = min(self.threads, threads or self.threads)
+        rc = self.L.refbatch_uniform(self._ctx, KINDS[self.kind], len(self._d), _p(self._d), batch, t, self.impl,
+                                     _p(a), _p(b), _p(ore), _p(oim))
+        if rc:
+            raise RuntimeError("reference afft batch failed")
+        return ore if self.kind == "ri" else (ore, oim)
+
+
+class RefMixed:
+    """Transforms of mixed shapes, each with its own arrays, through the
+    reference afft library's C API: host threads take them from a shared
+    counter, each keeping its own plans."""
+
+    def __init__(self, threads):
+        got = ref_bench_lib()
+        if got is None:
+            raise RuntimeError("reference afft library not built")
+        self.L, self.impl, self.what = got
+        self.threads = max(1, int(threads))
+        self._ctx = self.L.refbatch_ctx_create(self.threads)
+        self._keep = None
+
+    def __del__(self):
+        c = getattr(self, "_ctx", None)
+        if c:
+            self.L.refbatch_ctx_destroy(c)
+            self._ctx = None
+
+    def prepare(self, work):
+        """work: list of (kind, dims, a, b, out_a, out_b) with numpy float32
+        arrays (b / out_b None where the kind has none)."""
+        m = len(work)
+        kinds = np.array([KINDS[w[0]] for w in work], dtype=np.int32)
+        ndims = np.array([len(squeeze(w[1])) for w in work], dtype=np.int32)
+        dims = np.zeros((m, 3), dtype=np.uint64)
+        for i, w in enumerate(work):
+            d = squeeze(w[1])
+            dims[i, :len(d)] = d
+        ptr = lambda k: np.array([0 if w[k] is None else w[k].ctypes.data for w in work], dtype=np.uintp)
+        self._keep = (work, kinds, ndims, dims, ptr(2), ptr(3), ptr(4), ptr(5))
+        return m
+
+    def run(self):
+        work, kinds, ndims, dims, ia, ib, oa, ob = self._keep
+        rc = self.L.refbatch_mixed(self._ctx, len(work), _p(kinds), _p(ndims), _p(dims), _p(ia), _p(ib), _p(oa),
+                                   _p(ob), self.threads, self.impl)
+        if rc:
+            raise RuntimeError("reference afft mixed batch failed")

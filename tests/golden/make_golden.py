@@ -21,8 +21,17 @@ reference's double entry points (afft_64_*, fft.h:52-80).  Inputs are the
 same mt19937 floats (stored as float32, exact) widened to double; the output
 stored is afft_scalar's, and the json records how far afft_auto's differs.
 
-    python tests/golden/make_golden.py          # FP32 fixtures
-    python tests/golden/make_golden.py --f64    # FP64 fixtures
+With ``--configs`` it writes ``afft_golden_configs.npz`` / ``.json``: afft's
+float outputs (scalar backend and afft_auto) at the benchmark configurations'
+full sizes -- n=4096, n=65536, 256^3 complex, a 2^20-point real transform, and
+4096^2 real forward and inverse.  The inputs are not stored: they are the
+mt19937 uniform[-1,1) values of the case's seed, which the oracle's
+generator reproduces on any host.  Only the outputs at a seeded sample of
+4096 indices per array are stored, to keep the fixture small.
+
+    python tests/golden/make_golden.py            # FP32 fixtures
+    python tests/golden/make_golden.py --f64      # FP64 fixtures
+    python tests/golden/make_golden.py --configs  # config-size samples
 """
 import json
 import os
@@ -105,10 +114,65 @@ def main_f64():
     print("wrote %d FP64 cases" % len(index))
 
 
+# (name, kind, dims, seed) of the config-size cases
+CONFIG_CASES = [("c_4096", "c", [4096], 101), ("c_65536", "c", [65536], 102), ("c_256x256x256", "c", [256, 256, 256], 103),
+                ("r_1048576", "r", [1 << 20], 104), ("r_4096x4096", "r", [4096, 4096], 105),
+                ("ri_4096x4096", "ri", [4096, 4096], 106)]
+CONFIG_SAMPLE = 4096
+
+
+def config_inputs(kind, dims, seed):
+    """The inputs of a config-size case: mt19937(seed) uniform[-1,1)
+    floats, re block then im block (the harness's layout)."""
+    n = int(np.prod(dims))
+    h = O.half_elems(dims)
+    if kind in ("c", "ci"):
+        v = O.mt19937_uniform(2 * n, seed)
+        return v[:n], v[n:]
+    if kind == "r":
+        return O.mt19937_uniform(n, seed), None
+    v = O.mt19937_uniform(2 * h, seed)
+    return v[:h], v[h:]
+
+
+def config_sample_index(kind, dims, seed):
+    n = int(np.prod(dims))
+    m = O.half_elems(dims) if kind == "r" else n
+    return np.sort(np.random.default_rng(seed).choice(m, CONFIG_SAMPLE, replace=False)).astype(np.int64)
+
+
+def main_configs():
+    arrays = {}
+    index = []
+    for name, kind, dims, seed in CONFIG_CASES:
+        a, b = config_inputs(kind, dims, seed)
+        idx = config_sample_index(kind, dims, seed)
+        arrays[name + "/index"] = idx
+        for tag, impl in (("scalar", AFFT_SCALAR), ("auto", AFFT_AUTO)):
+            out = O.ref_run(kind, dims, a, b, impl)
+            if kind == "ri":
+                arrays[name + "/%s0" % tag] = out[idx]
+            else:
+                arrays[name + "/%s0" % tag] = out[0][idx]
+                arrays[name + "/%s1" % tag] = out[1][idx]
+        index.append({"name": name, "kind": kind, "dims": dims, "seed": seed, "sample": CONFIG_SAMPLE})
+        print(name, flush=True)
+    np.savez_compressed(os.path.join(HERE, "afft_golden_configs.npz"), **arrays)
+    with open(os.path.join(HERE, "afft_golden_configs.json"), "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py --configs",
+                   "reference_impls": {"scalar": AFFT_SCALAR, "auto": AFFT_AUTO},
+                   "inputs": "mt19937(seed) uniform[-1,1) floats (oracle.mt19937_uniform), re block then im block",
+                   "outputs": "sampled at the stored indices (np.random.default_rng(seed).choice, sorted)",
+                   "cases": index}, f, indent=1)
+    print("wrote %d config-size cases" % len(index))
+
+
 def main():
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "all", "ref"], check=True)
     if "--f64" in sys.argv[1:]:
         return main_f64()
+    if "--configs" in sys.argv[1:]:
+        return main_configs()
     arrays = {}
     index = []
     for name, kind, dims, seed in cases():

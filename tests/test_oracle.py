@@ -146,3 +146,21 @@ def test_port64_against_reference_fp64_outputs(golden64):
         identical += all(np.array_equal(x, y) for x, y in zip(gg, rr))
     assert identical >= len(cases) // 2, identical
     print("port64 bit-identical to afft_64 scalar on %d of %d cases" % (identical, len(cases)))
+
+
+@pytest.mark.parametrize("i", range(6))
+def test_oracle64_against_reference_outputs_at_config_sizes(golden_configs, i):
+    # the FP64 oracle against afft's own outputs at the benchmark sizes
+    # (n=4096, 65536, 256^3, 2^20 real, 4096^2 real and its inverse), on the
+    # stored sample of output indices; afft's own error there is ~5e-7
+    from conftest import config_case_inputs
+    z, cases = golden_configs
+    case = cases[i]
+    nm, kind, dims = case["name"], case["kind"], case["dims"]
+    a, b = config_case_inputs(case)
+    o = O.oracle64(kind, dims, a, b)
+    idx = z[nm + "/index"]
+    osmp = o[idx] if kind == "ri" else (o[0][idx], o[1][idx])
+    for tag in ("scalar", "auto"):
+        out = z[nm + "/%s0" % tag] if kind == "ri" else (z[nm + "/%s0" % tag], z[nm + "/%s1" % tag])
+        assert O.rel_l2(out, osmp) <= 2e-6, (nm, tag)

@@ -129,6 +129,25 @@ def test_golden_cases(golden, dev):
     print("worst rel-L2 vs FP64 over golden cases: %.2e" % worst)
 
 
+@pytest.mark.parametrize("i", range(6), ids=["c_4096", "c_65536", "c_256^3", "r_2^20", "r_4096^2", "ri_4096^2"])
+def test_golden_config_sizes(golden_configs, dev, i):
+    # afft's own float outputs at the benchmark sizes (stored at a sample of
+    # 4096 indices per array), against the GPU result through the C ABI on
+    # the same mt19937 inputs
+    from conftest import config_case_inputs
+    z, cases = golden_configs
+    case = cases[i]
+    nm, kind, dims = case["name"], case["kind"], case["dims"]
+    a, b = config_case_inputs(case)
+    got = run_plan(kind, dims, a, b, dev)
+    idx = z[nm + "/index"]
+    gs = got[idx] if kind == "ri" else (got[0][idx], got[1][idx])
+    for tag in ("scalar", "auto"):
+        ref = z[nm + "/%s0" % tag] if kind == "ri" else (z[nm + "/%s0" % tag], z[nm + "/%s1" % tag])
+        err = O.rel_l2(gs, ref)
+        assert err <= TOL, (nm, tag, err)
+
+
 def test_c1_harness_input_and_round_trip(golden, dev):
     z, _ = golden
     a, b = z["c1/in0"], z["c1/in1"]
