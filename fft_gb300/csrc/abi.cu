@@ -271,15 +271,16 @@ static void io_elems(const Plan& P, long long* in_n, long long* out_n) {
   *out_n = P.out_elems * P.batch;
 }
 
-// A TC-form kernel whose bounded wait for its tensor-core results gave up
+// A kernel whose bounded wait gave up (a TC-form kernel waiting for its
+// tensor-core results: 1; a cols pass waiting for its TMA-loaded tile: 2)
 // sets the device error word instead of hanging; report and clear it.
 static int check_tc_error(const Plan& P) {
-  if (P.form != FORM_TC) return 0;
+  if (P.form != FORM_TC && !P.has_tma) return 0;
   int* w = tc_error_word();
   int v = 0;
   if (w && cudaMemcpy(&v, w, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess && v) {
     cudaMemset(w, 0, sizeof(int));
-    set_error(AFFT_GB300_ETIMEOUT, "tensor-core stage wait timed out");
+    set_error(AFFT_GB300_ETIMEOUT, v == 2 ? "TMA tile wait timed out" : "tensor-core stage wait timed out");
     return AFFT_GB300_ETIMEOUT;
   }
   return 0;

@@ -7,6 +7,7 @@ namespace agb {
 
 typedef void (*LineKernelFn)(LineParams);
 typedef void (*GroupedKernelFn)(const Segment*, const int*, long long);
+typedef void (*LineKernelTmaFn)(LineParams, TmaTile);
 
 struct LineKernel {
   LineKernelFn fn;
@@ -23,6 +24,8 @@ struct LineKernel {
   size_t smem;         // bytes of dynamic shared memory
   int halves;          // CTAs per tile of C lines (2: the split R2C pass)
   int stage_logl;      // log2 length of the stage twiddle table the kernel reads
+  LineKernelTmaFn tma; // the same pass with its input tile loaded by TMA (cols passes over
+                       // split planes), or null
 };
 
 constexpr int ROWS_MAX_LOG = 14;   // rows mode: one CTA up to 16384 points
@@ -57,6 +60,11 @@ bool get_rows_real_pairs(int logl, int kind, LineKernel* out);
 bool get_line_kernel64(int logl, bool cols, int kind, bool tstore, LineKernel* out);
 bool get_rows64(int logl, int kind, LineKernel* out);
 bool get_cols64(int logl, int kind, bool tstore, LineKernel* out);
+
+// cols passes {C2C, R2C, C2R} of 2^8 .. 2^11 points whose input tile is
+// loaded by TMA (line_fft_tma); out->tma set, the rest as the LSU kernel
+// of the same shape (the R2C pass of 2^11 points unsplit: one CTA per tile)
+bool get_cols_tma(int logl, int kind, LineKernel* out);
 
 // split-precision tensor-core form: rows c2c L = 256 or 4096, cols c2c L = 256
 bool get_tc_kernel(int logl, bool cols, bool tstore, LineKernel* out);
@@ -100,13 +108,15 @@ constexpr int lines_per_cta_k() {
   else return lines_per_cta<LOGL, COLS>();
 }
 
-template <int LOGL, bool COLS, int KIND, bool TSTORE, bool TC = false, int UNIT = 0>
+// CC: lines per CTA when not the measured default of lines_per_cta_k
+template <int LOGL, bool COLS, int KIND, bool TSTORE, bool TC = false, int UNIT = 0, int CC = 0>
 LineKernel make_line_kernel() {
-  constexpr int C = lines_per_cta_k<LOGL, COLS, KIND>();
+  constexpr int C = CC ? CC : lines_per_cta_k<LOGL, COLS, KIND>();
   static_assert(!TC || (size_t)LineSmem<LOGL, C, COLS, TSTORE, TC>::FLOAT2S * 8 >= (size_t)(Sched<LOGL>::T * C / 128) * 16384,
                 "TC operand tiles must fit in the exchange buffer");
   LineKernel k;
   k.fn = &line_fft<LOGL, C, COLS, KIND, TSTORE, TC, UNIT>;
+  k.tma = nullptr;
   k.grouped = &line_fft_grouped<LOGL, C, COLS, KIND, TSTORE, TC, UNIT>;
   k.tc = TC;
   k.unit = UNIT;
@@ -120,6 +130,19 @@ LineKernel make_line_kernel() {
   k.lines_per_cta = C;
   k.threads = Sched<LOGL>::T * C;
   k.smem = (size_t)LineSmem<LOGL, C, COLS, TSTORE, TC>::FLOAT2S * sizeof(float2);
+  return k;
+}
+
+// a cols pass with its TMA-fed variant (CC: lines per CTA, 0 = the default)
+template <int LOGL, int KIND, int CC = 0>
+LineKernel make_tma_kernel() {
+  constexpr int C = CC ? CC : lines_per_cta_k<LOGL, true, KIND>();
+  static_assert((size_t)LineSmem<LOGL, C, true, false, false>::FLOAT2S * sizeof(float2) >=
+                    (size_t)2 * (1 << LOGL) * C * sizeof(float),
+                "the input tile fits the exchange buffer it aliases");
+  static_assert(C * sizeof(float) % 16 == 0, "tile columns span whole 16-byte units");
+  LineKernel k = make_line_kernel<LOGL, true, KIND, false, false, 0, C>();
+  k.tma = &line_fft_tma<LOGL, C, KIND>;
   return k;
 }
 

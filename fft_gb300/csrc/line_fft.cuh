@@ -37,6 +37,7 @@
 // afft uses for its inverse plans (common.hpp:355-378).
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -888,8 +889,12 @@ __device__ __forceinline__ void rows_stage_out_reals(const LineParams& p, long l
 // products.  Cols mode: bit 0 the input, bit 1 the output are
 // interleaved pairs (im = re + 1, even strides), accessed as float2 (the
 // paired R2C pass: bit 0 only; the paired C2R pass: bit 1 only).
-template <int LOGL, int C, bool COLS, int KIND, bool TSTORE, bool TC = false, int UNIT = 0>
+// TMA: the CTA's input tile is already in the exchange buffer, put there by
+// tma_load_tile (cols mode, split planes): [re: L rows x C][im: L rows x C]
+// floats; C2R tiles hold bins 0 .. L-1 there and read bin L directly.
+template <int LOGL, int C, bool COLS, int KIND, bool TSTORE, bool TC = false, int UNIT = 0, bool TMA = false>
 __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta, TcState* ts = nullptr) {
+  static_assert(!TMA || (COLS && !TC && UNIT == 0 && !TSTORE), "TMA tiles: plain cols passes over split planes");
   if constexpr (KIND == LK_R2C_HALF) {
     static_assert(COLS && !TSTORE && !TC, "the split R2C pass is a plain cols pass");
     r2c_half_body<LOGL, C>(p, cta);
@@ -934,7 +939,34 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
         staged = true;
       }
     }
-    if (staged) {
+    if constexpr (TMA) {
+      // bins from the tile: bin i of column c at raw[i C + c] (re plane) and
+      // raw[L C + i C + c] (im plane); bin L (the mirror of bin 0) from HBM
+      const float* raw = reinterpret_cast<const float*>(smem_raw);
+      float2 bl = make_float2(0.f, 0.f);
+      if (t == 0 && active) {
+        const long long oL = line_off(p.in, q) + (long long)L * p.in.es;
+        bl = make_float2(__ldg(p.in.re + oL), __ldg(p.in.im + oL));
+      }
+#pragma unroll
+      for (int e = 0; e < E; e++) {
+        const int i = t + T * e;
+        const float2 s0 = make_float2(raw[i * C + c], raw[L * C + i * C + c]);
+        const int im = (L - i) & (L - 1);
+        const float2 s1 = i == 0 ? bl : make_float2(raw[im * C + c], raw[L * C + im * C + c]);
+        float2 z;
+        if (i == 0) {
+          z = make_float2(s0.x + s1.x, s0.x - s1.x);
+        } else {
+          float2 w = ldg2(p.rtw + i);
+          float2 a = cadd(s0, cconj(s1));
+          float2 b = cmul(csub(cconj(s1), s0), cconj(w));
+          z = cadd(a, cmul_negi(b));
+        }
+        v[e] = cswap(z);
+      }
+      __syncthreads();   // the tile is read before the stages reuse the buffer
+    } else if (staged) {
     } else if (active) {
       // bin i = t + T e at p0 + e S, its mirror L - i at p1 - e S
       const long long base = line_off(p.in, q);
@@ -988,7 +1020,21 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
         for (int e = 0; e < E; e++) v[e] = cswap(v[e]);
       }
     }
-    if (staged) {
+    if constexpr (TMA) {
+      // element i of column c at raw[i C + c] (re plane), raw[L C + i C + c]
+      // (im plane): a warp's 32 lanes read 32 consecutive words
+      const float* raw = reinterpret_cast<const float*>(smem_raw);
+#pragma unroll
+      for (int e = 0; e < E; e++) {
+        const int i = t + T * e;
+        v[e] = make_float2(raw[i * C + c], raw[L * C + i * C + c]);
+      }
+      if (p.inverse) {
+#pragma unroll
+        for (int e = 0; e < E; e++) v[e] = cswap(v[e]);
+      }
+      __syncthreads();   // the tile is read before the stages reuse the buffer
+    } else if (staged) {
     } else if (active) {
       const long long base = line_off(p.in, q);
       if constexpr (RU == 1) {
@@ -1345,6 +1391,84 @@ line_fft(const LineParams p) {
   } else {
     line_fft_body<LOGL, C, COLS, KIND, TSTORE, false, UNIT>(p, blockIdx.x);
   }
+}
+
+// ---------------------------------------------------------------------------
+// TMA-fed cols passes
+// ---------------------------------------------------------------------------
+// A cols tile of C lines reads C * 4 bytes (32 for C = 8) of each row it
+// touches.  Through the LSU every load wavefront then carries one 32-byte
+// segment, and the 1024- and 2048-point passes saturate L1 (74-84% of its
+// throughput for 25% of HBM's).  Here one thread loads the CTA's whole input
+// tile with tensor-map copies (cp.async.bulk.tensor, 3D boxes of C columns x
+// BR rows) into the exchange buffer, completing on an mbarrier; the threads
+// then read their canonical elements from shared memory.
+//
+// The maps (encoded on the host per launch) view a plane of the input as
+// {columns of one outer block, L rows (stride es), outer blocks (stride
+// hi)}: line q = o * ncols + col is column col of block o, and a CTA's C
+// lines are C adjacent columns of one block.  Both planes' bases, es * 4 and
+// hi * 4 are multiples of 16 bytes and the column of a tile is a multiple of
+// C (>= 4 floats), so every box starts on a 16-byte boundary.
+struct TmaTile {
+  CUtensorMap re, im;   // the input's re and im planes
+  int box_rows;         // rows per box (<= 256, divides L)
+  int rows;             // rows loaded per plane (L)
+};
+
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int x, int y, int z,
+                                            uint32_t mbar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::
+          "r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(mbar)
+      : "memory");
+}
+
+// Loads the tile of CTA `cta` into dst ([re rows][C] then [im rows][C]
+// floats).  Every thread waits, bounded; on a timeout the error word is set,
+// the copies get a second bounded wait, and the whole CTA returns false.
+template <int C>
+__device__ __forceinline__ bool tma_load_tile(const LineParams& p, const TmaTile& tm, long long cta, uint64_t* mbar,
+                                              void* dst) {
+  const uint32_t mb = smem_u32(mbar);
+  const long long q0 = cta * C;
+  const int col = (int)(q0 & p.in.qmask);
+  const int outer = (int)(q0 >> p.in.qshift);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint32_t bytes = 2u * (uint32_t)tm.rows * C * 4u;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(bytes) : "memory");
+    const uint32_t d = smem_u32(dst);
+    const uint32_t plane = (uint32_t)tm.rows * C * 4u;
+    for (int r = 0; r < tm.rows; r += tm.box_rows) {
+      tma_load_3d(d + (uint32_t)r * C * 4u, &tm.re, col, r, outer, mb);
+      tma_load_3d(d + plane + (uint32_t)r * C * 4u, &tm.im, col, r, outer, mb);
+    }
+  }
+  const bool ok = __syncthreads_and(tc_wait(mb, 0));
+  if (!ok) {
+    if (threadIdx.x == 0) {
+      if (p.err) atomicExch(p.err, 2);
+      tc_wait(mb, 0);   // let copies still in flight land before the CTA's shared memory goes away
+    }
+    __syncthreads();
+  }
+  return ok;
+}
+
+template <int LOGL, int C, int KIND>
+__global__ void __launch_bounds__(Sched<LOGL>::T * C, min_ctas<Sched<LOGL>::T * C>())
+line_fft_tma(const LineParams p, const __grid_constant__ TmaTile tm) {
+  __shared__ __align__(8) uint64_t mbar;
+  extern __shared__ __align__(1024) float2 smem_raw[];
+  if (!tma_load_tile<C>(p, tm, blockIdx.x, &mbar, smem_raw)) return;
+  line_fft_body<LOGL, C, true, KIND, false, false, 0, true>(p, blockIdx.x);
 }
 
 // One launch of a multi-transform queue: a device-side table of segments

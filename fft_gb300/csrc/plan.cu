@@ -25,6 +25,8 @@
 #include <mutex>
 
 #include "plan.h"
+
+#include <cudaTypedefs.h>
 #include "line_fft64.cuh"
 
 namespace agb {
@@ -349,6 +351,26 @@ static View inter_view(int b, long long off = 0) {  // re,im pairs in one array
 // Four-step split L = L1 * L2: L1 (the first, transposing pass) takes the
 // larger half for odd log2 L (measured the better split on GB300).
 #define AFFT_L1(logl) (((logl) + 1) / 2)
+// cols passes take their TMA-fed kernels where one exists (0: LSU loads only)
+#ifndef AFFT_COLS_TMA
+#define AFFT_COLS_TMA 1
+#endif
+// ... and of the 2048-point passes, per kind.  There one CTA fills an SM
+// (128 KB tiles), so a TMA-loaded tile cannot overlap another CTA's work:
+// measured on GB300, the C2C pass is 3% slower with TMA (2048^2 x 8: 0.2628
+// vs 0.2710 ms), the unsplit R2C pass 7-9% slower than the split LSU form
+// (4096^2 r2c: 0.0826 vs 0.0897 ms), 4-line tiles slower still; the C2R
+// pass, whose LSU form reads every bin twice, 9% faster (4096^2 c2r: 0.0959
+// vs 0.0867 ms).
+#ifndef AFFT_TMA_C2C11
+#define AFFT_TMA_C2C11 0
+#endif
+#ifndef AFFT_TMA_R2C11
+#define AFFT_TMA_R2C11 0
+#endif
+#ifndef AFFT_TMA_C2R11
+#define AFFT_TMA_C2R11 1
+#endif
 
 static IOSpec io(const View& v, long long es, long long lo, long long hi, int qshift, long long qmask) {
   IOSpec s;
@@ -434,6 +456,20 @@ struct Builder {
       fail("no kernel for this line length");
       return;
     }
+    // cols passes over split planes: the variant with TMA-loaded input tiles
+    // (taken at launch when the bound arrays meet its alignment rules)
+    if (AFFT_COLS_TMA && !f64 && !tc && cols && !tstore && !cpairs && !tune.cols_lsu &&
+        (kind == LK_C2C || kind == LK_R2C || kind == LK_C2R)) {
+      LineKernel kt;
+      // (the 2048-point R2C pass: unsplit, one CTA per tile, replacing the
+      // split form; its LSU kernel is the fallback)
+      // (kernels compare by shape: each translation unit has its own host
+      // stub of a template kernel, so their addresses differ)
+      const bool want = logl < 11 || (kind == LK_C2C ? AFFT_TMA_C2C11 : kind == LK_R2C ? AFFT_TMA_R2C11 : AFFT_TMA_C2R11);
+      if (want && get_cols_tma(logl, kind, &kt) && kt.kind == op.k.kind && kt.logl == op.k.logl &&
+          kt.unit == op.k.unit && !op.k.tstore && !op.k.tc)
+        op.k = kt;
+    }
     op.in = in;
     op.out = out;
     op.p.nlines = nlines;
@@ -444,11 +480,21 @@ struct Builder {
     op.p.tw_qshift = tw_qshift;
     if (!dry) {
       if (op.k.smem > 48 * 1024 &&
-          cudaFuncSetAttribute((const void*)op.k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)op.k.smem) != cudaSuccess) {
+          (cudaFuncSetAttribute((const void*)op.k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)op.k.smem) != cudaSuccess ||
+           (op.k.tma && cudaFuncSetAttribute((const void*)op.k.tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)op.k.smem) != cudaSuccess))) {
         cudaGetLastError();
         fail("kernel shared memory configuration failed");
         return;
+      }
+      if (op.k.tma) {
+        op.p.err = tc_error_word();
+        if (!op.p.err) {
+          fail("error word allocation failed");
+          return;
+        }
+        P.has_tma = true;
       }
       if (f64) {
         // the FP64 kernels read double2 tables through the same fields
@@ -815,11 +861,11 @@ std::string describe_plan(const Plan& P) {
     if (op.type == OP_LINE) {
       snprintf(buf, sizeof buf,
                "{\"type\":\"line\",\"logl\":%d,\"cols\":%d,\"lk\":%d,\"tstore\":%d,\"tc\":%d,\"C\":%d,"
-               "\"halves\":%d,\"unit\":%d,"
+               "\"halves\":%d,\"unit\":%d,\"tma\":%d,"
                "\"threads\":%d,\"smem\":%zu,\"grid\":%lld,\"nlines\":%lld,\"inverse\":%d,"
                "\"tw_n\":%lld,\"tw_qmask\":%lld,\"tw_qshift\":%d,\"real_L\":%lld,\"pcols\":%lld,",
                op.k.logl, op.k.cols, op.k.kind, op.k.tstore, op.k.tc, op.k.lines_per_cta, op.k.halves, op.k.unit,
-               op.threads,
+               op.k.tma != nullptr, op.threads,
                op.smem,
                op.grid, op.p.nlines, op.p.inverse, op.p.tw_n, op.p.tw_qmask, op.p.tw_qshift, op.real_L, op.p.pcols);
     } else if (op.type == OP_REAL) {
@@ -868,6 +914,53 @@ static LineIO bind(const IOSpec& s, float* const* base, size_t esz) {
   return o;
 }
 
+// The driver's tensor-map encoder, looked up once.
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      f = nullptr;
+    }
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+  }();
+  return fn;
+}
+
+// The tensor maps of a cols pass's input planes, when the bound arrays
+// allow them: lines are whole tiles of C adjacent columns of one outer block
+// (lo = 1, ncols = 2^qshift a multiple of C, every block whole), both plane
+// bases 16-byte aligned, row and block strides multiples of 16 bytes.  Boxes
+// of C columns x min(L, 256) rows.  false: launch the LSU kernel instead.
+bool tma_tile(const LineParams& p, const LineKernel& k, TmaTile* tm) {
+  const LineIO& in = p.in;
+  const long long L = 1LL << k.logl, C = k.lines_per_cta;
+  const long long ncols = in.qmask + 1;
+  if (in.lo != 1 || ncols != (1LL << in.qshift) || ncols % C || p.nlines % ncols || L > (1LL << 16)) return false;
+  if ((reinterpret_cast<uintptr_t>(in.re) | reinterpret_cast<uintptr_t>(in.im)) & 15) return false;
+  const long long nouter = p.nlines / ncols;
+  const long long rs = in.es * 4, bs = nouter > 1 ? in.hi * 4 : L * in.es * 4;
+  if (rs % 16 || bs % 16 || rs <= 0 || bs <= 0 || rs >= (1LL << 40) || bs >= (1LL << 40)) return false;
+  auto encode = tensor_map_encoder();
+  if (!encode) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)ncols, (cuuint64_t)L, (cuuint64_t)nouter};
+  const cuuint64_t strides[2] = {(cuuint64_t)rs, (cuuint64_t)bs};
+  const int br = (int)std::min<long long>(L, 256);
+  const cuuint32_t box[3] = {(cuuint32_t)C, (cuuint32_t)br, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  for (int i = 0; i < 2; i++) {
+    if (encode(i ? &tm->im : &tm->re, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)(i ? in.im : in.re), dims, strides,
+               box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return false;
+  }
+  tm->box_rows = br;
+  tm->rows = (int)L;
+  return true;
+}
+
 bool op_tables_ok(const Op& op) {
   if (op.type != OP_LINE) return op.type != OP_REAL || op.rp.rtw;
   return op.p.tw && (op.k.kind == LK_C2C || op.p.rtw) &&
@@ -898,7 +991,12 @@ int Plan::launch(const float* src_re, const float* src_im, float* dst_re, float*
       LineParams p = op.p;
       p.in = bind(op.in, base, esz);
       p.out = bind(op.out, base, esz);
-      op.k.fn<<<(unsigned)op.grid, op.threads, op.smem, st>>>(p);
+      TmaTile tm;
+      if (op.k.tma && tma_tile(p, op.k, &tm)) {
+        op.k.tma<<<(unsigned)op.grid, op.threads, op.smem, st>>>(p, tm);
+      } else {
+        op.k.fn<<<(unsigned)op.grid, op.threads, op.smem, st>>>(p);
+      }
     } else if (op.type == OP_REAL) {
       RealPassParams rp = op.rp;
       rp.in = bind(op.in, base, esz);

@@ -59,6 +59,7 @@ constexpr int FORM_F64 = 0x200;
 
 struct Plan {
   int kind = K_C;
+  bool has_tma = false;        // some op may take its TMA-fed kernel (its waits report through the error word)
   int format = 0;              // afft_split / afft_interleaved
   int form = 0;                // 0 plain FP32, FORM_TC split-precision tensor cores, FORM_F64 FP64
   int ndim = 1;
@@ -94,10 +95,12 @@ struct Plan {
 // Plan variants the autotuner chooses between (tune.cu).  split: 0 the
 // built-in four-step split of long axes, 1 the other half first; real_inv:
 // 0 the fused paired pre-pass for long 1D real inverses where it applies,
-// 1 the standalone pre-pass.
+// 1 the standalone pre-pass; cols_lsu: 0 TMA-loaded input tiles for the
+// cols passes that have them, 1 the LSU loads.
 struct Tuning {
   int split = 0;
   int real_inv = 0;
+  int cols_lsu = 0;   // 1: cols passes load their tiles through the LSU even where TMA applies
 };
 // The tuned choice for a shape on the current device, if the autotuner has
 // one (tuning it first when AFFT_GB300_AUTOTUNE=1); else the defaults.
@@ -113,6 +116,10 @@ std::unique_ptr<Plan> build_plan(int kind, int ndim, const long long* dims, long
 // TC form: the DFT-16 matrix tiles (Mh, Ml) and the per-device error word
 const __half* tc_matrix_table();
 int* tc_error_word();
+
+// The tensor maps of a cols pass's TMA-fed kernel for the bound arrays, or
+// false when they do not meet its alignment rules (launch k.fn instead).
+bool tma_tile(const LineParams& p, const LineKernel& k, TmaTile* tm);
 
 // Whether every table an op's kernel reads is present (device plans).
 bool op_tables_ok(const Op& op);
