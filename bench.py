@@ -737,6 +737,34 @@ def measure_queue(args, cfg, dev, steps=None, soak=None, cpu=True, e2e=True, tc=
         q.run(stream)           # leave the plain form's outputs in place
         torch.cuda.synchronize()
 
+    # the same queue with the autotuner's per-shape choices (each distinct
+    # shape tuned on this device when the queue is created)
+    tunedrec = None
+    if tc and args.form == "plain" and not args.no_tune:
+        t0 = time.perf_counter()
+        qq = G.Queue(U.descs(items, buf, offs), tuned=True)
+        tune_s = time.perf_counter() - t0
+        for _ in range(3):
+            qq.run(stream)
+        torch.cuda.synchronize()
+        t0e, t1e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0e.record(stream)
+        for _ in range(steps):
+            qq.run(stream)
+        t1e.record(stream)
+        torch.cuda.synchronize()
+        ms_tuned = t0e.elapsed_time(t1e) / steps
+        tunedrec = {"ms_per_step": round(ms_tuned, 4), "transforms_per_s": round(len(items) / (ms_tuned / 1e3), 1),
+                    "untuned_ms_per_step": round(ms, 4), "ratio_to_untuned": round(ms / ms_tuned, 3),
+                    "tuning_s": round(tune_s, 1), "launches_per_step": qq.launches,
+                    "accuracy": queue_accuracy(items, buf, offs, sample_idx),
+                    "note": "each distinct (kind, shape) tuned at a batch of about 2^24 elements: four-step split, "
+                            "real pre-pass placement, TMA or LSU tile loads, cols tile width, plain or "
+                            "tensor-core form"}
+        del qq
+        q.run(stream)           # leave the plain form's outputs in place
+        torch.cuda.synchronize()
+
     # end to end: every step copies all inputs from pinned host memory, runs
     # the queue and copies all outputs back (one copy each way: the inputs
     # and the outputs occupy two contiguous regions).  Steps are pipelined the
@@ -787,7 +815,7 @@ def measure_queue(args, cfg, dev, steps=None, soak=None, cpu=True, e2e=True, tc=
            "roofline": {"bound": "hbm", "achieved": round(by / (ms / 1e3) / 1e9, 1), "peak": hbm, "unit": "GB/s",
                         "frac": round(by / (ms / 1e3) / 1e9 / hbm, 4), "traffic": None, "peak_source": peak_src,
                         "kernel": "whole queue (graph of %d launches)" % q.launches},
-           "accuracy": acc, "tc_split_form": tcrec, "e2e": e2erec, "cpu_baseline": cpurec,
+           "accuracy": acc, "tc_split_form": tcrec, "autotuned": tunedrec, "e2e": e2erec, "cpu_baseline": cpurec,
            "gpu_launches": q.launches * steps,
            "clocks": dict(clk.summary(), window="soak %.1f s + timed region" % soak)}
     del q, buf
@@ -849,6 +877,7 @@ def run_ours(args, cfg):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": DATA,
                 "config": config_record(cfg, args), "roofline": rec["roofline"], "cpu_baseline": rec["cpu_baseline"],
                 "e2e": rec["e2e"], "accuracy": rec["accuracy"], "tc_split_form": rec["tc_split_form"],
+                "autotuned": rec["autotuned"],
                 "transforms_per_s": rec["transforms_per_s"], "queue_launches": rec["queue_launches"],
                 "gpu_launches": rec["gpu_launches"], "clocks": rec["clocks"]}
         print(json.dumps(line), flush=True)
@@ -931,6 +960,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tc", action="store_true", help="skip timing the tensor-core form beside the plain one")
     ap.add_argument("--no-sub", action="store_true", help="headline configuration only (no \"configs\" records)")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuned queue beside the default one")
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--sub-cpu-budget", type=float, default=3.0,
                     help="seconds of CPU baseline per configuration record")

@@ -25,6 +25,7 @@ afft_split, afft_interleaved = 0, 1
 KIND_C, KIND_CI, KIND_R, KIND_RI = 0, 1, 2, 3
 FORM_TC = 0x100   # AFFT_GB300_FORM_TC: split-precision tensor-core butterflies
 FORM_F64 = 0x200  # AFFT_GB300_FORM_F64: FP64 data and arithmetic (the afft_64_* path)
+QUEUE_TUNED = 0x400  # AFFT_GB300_QUEUE_TUNED: queue plans take the autotuner's per-shape choices
 KINDS = {"c": KIND_C, "ci": KIND_CI, "r": KIND_R, "ri": KIND_RI}
 ERRORS = {0: "OK", 1: "EINVAL", 2: "ENODEV", 3: "ENOMEM", 4: "ECUDA", 5: "ESTATE", 6: "ETIMEOUT"}
 
@@ -418,7 +419,7 @@ class Queue:
     device arrays.
     """
 
-    def __init__(self, descs, form=None):
+    def __init__(self, descs, form=None, tuned=False):
         items = list(descs)
         arr = (Desc * max(1, len(items)))()
         for i, (kind, dims, sr, si, dr, di) in enumerate(items):
@@ -428,7 +429,8 @@ class Queue:
             for j, x in enumerate(dims[:3]):
                 d.dim[j] = int(x)
             d.src_re, d.src_im, d.dst_re, d.dst_im = ptr(sr), ptr(si), ptr(dr), ptr(di)
-        self._q = lib().afft_gb300_queue_create_ex(arr, len(items), FORM_TC if form == "tc" else 0)
+        flags = (FORM_TC if form == "tc" else 0) | (QUEUE_TUNED if tuned else 0)
+        self._q = lib().afft_gb300_queue_create_ex(arr, len(items), flags)
         if not self._q:
             _check("queue_create")
             raise AfftError("queue_create failed")

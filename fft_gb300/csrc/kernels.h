@@ -26,6 +26,7 @@ struct LineKernel {
   int stage_logl;      // log2 length of the stage twiddle table the kernel reads
   LineKernelTmaFn tma; // the same pass with its input tile loaded by TMA (cols passes over
                        // split planes), or null
+  GroupedKernelFn grouped_tma;   // its grouped form (queue segments with tensor maps), or null
 };
 
 constexpr int ROWS_MAX_LOG = 14;   // rows mode: one CTA up to 16384 points
@@ -65,6 +66,14 @@ bool get_cols64(int logl, int kind, bool tstore, LineKernel* out);
 // loaded by TMA (line_fft_tma); out->tma set, the rest as the LSU kernel
 // of the same shape (the R2C pass of 2^11 points unsplit: one CTA per tile)
 bool get_cols_tma(int logl, int kind, LineKernel* out);
+// the transposing-store complex cols passes (four-step pass A) of 2^8 ..
+// 2^10 points with TMA-loaded input tiles (k_cols_tma_ts.cu)
+bool get_cols_tma_tstore(int logl, LineKernel* out);
+
+// cols c2c passes (not transposing) with another tile width, for the
+// autotuner: 256 points in 8 or 32 lines, 512 points in 16; TMA-fed
+// variant included (k_cols_alt.cu)
+bool get_cols_c2c_alt(int logl, int lines, LineKernel* out);
 
 // split-precision tensor-core form: rows c2c L = 256 or 4096, cols c2c L = 256
 bool get_tc_kernel(int logl, bool cols, bool tstore, LineKernel* out);
@@ -117,6 +126,7 @@ LineKernel make_line_kernel() {
   LineKernel k;
   k.fn = &line_fft<LOGL, C, COLS, KIND, TSTORE, TC, UNIT>;
   k.tma = nullptr;
+  k.grouped_tma = nullptr;
   k.grouped = &line_fft_grouped<LOGL, C, COLS, KIND, TSTORE, TC, UNIT>;
   k.tc = TC;
   k.unit = UNIT;
@@ -134,15 +144,16 @@ LineKernel make_line_kernel() {
 }
 
 // a cols pass with its TMA-fed variant (CC: lines per CTA, 0 = the default)
-template <int LOGL, int KIND, int CC = 0>
+template <int LOGL, int KIND, int CC = 0, bool TSTORE = false>
 LineKernel make_tma_kernel() {
   constexpr int C = CC ? CC : lines_per_cta_k<LOGL, true, KIND>();
-  static_assert((size_t)LineSmem<LOGL, C, true, false, false>::FLOAT2S * sizeof(float2) >=
+  static_assert((size_t)LineSmem<LOGL, C, true, TSTORE, false>::FLOAT2S * sizeof(float2) >=
                     (size_t)2 * (1 << LOGL) * C * sizeof(float),
                 "the input tile fits the exchange buffer it aliases");
   static_assert(C * sizeof(float) % 16 == 0, "tile columns span whole 16-byte units");
-  LineKernel k = make_line_kernel<LOGL, true, KIND, false, false, 0, C>();
-  k.tma = &line_fft_tma<LOGL, C, KIND>;
+  LineKernel k = make_line_kernel<LOGL, true, KIND, TSTORE, false, 0, C>();
+  k.tma = &line_fft_tma<LOGL, C, KIND, TSTORE>;
+  k.grouped_tma = &line_fft_grouped<LOGL, C, true, KIND, TSTORE, false, 0, true>;
   return k;
 }
 

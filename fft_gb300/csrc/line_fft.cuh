@@ -894,7 +894,8 @@ __device__ __forceinline__ void rows_stage_out_reals(const LineParams& p, long l
 // floats; C2R tiles hold bins 0 .. L-1 there and read bin L directly.
 template <int LOGL, int C, bool COLS, int KIND, bool TSTORE, bool TC = false, int UNIT = 0, bool TMA = false>
 __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta, TcState* ts = nullptr) {
-  static_assert(!TMA || (COLS && !TC && UNIT == 0 && !TSTORE), "TMA tiles: plain cols passes over split planes");
+  static_assert(!TMA || (COLS && !TC && UNIT == 0 && (!TSTORE || KIND == LK_C2C)),
+                "TMA tiles: cols passes over split planes");
   if constexpr (KIND == LK_R2C_HALF) {
     static_assert(COLS && !TSTORE && !TC, "the split R2C pass is a plain cols pass");
     r2c_half_body<LOGL, C>(p, cta);
@@ -1452,6 +1453,9 @@ __device__ __forceinline__ bool tma_load_tile(const LineParams& p, const TmaTile
     }
   }
   const bool ok = __syncthreads_and(tc_wait(mb, 0));
+  // every thread has passed the wait: the barrier may be set up again by a
+  // later tile of the same CTA (grouped launches)
+  if (ok && threadIdx.x == 0) asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(mb) : "memory");
   if (!ok) {
     if (threadIdx.x == 0) {
       if (p.err) atomicExch(p.err, 2);
@@ -1462,13 +1466,13 @@ __device__ __forceinline__ bool tma_load_tile(const LineParams& p, const TmaTile
   return ok;
 }
 
-template <int LOGL, int C, int KIND>
+template <int LOGL, int C, int KIND, bool TSTORE = false>
 __global__ void __launch_bounds__(Sched<LOGL>::T * C, min_ctas<Sched<LOGL>::T * C>())
 line_fft_tma(const LineParams p, const __grid_constant__ TmaTile tm) {
   __shared__ __align__(8) uint64_t mbar;
   extern __shared__ __align__(1024) float2 smem_raw[];
   if (!tma_load_tile<C>(p, tm, blockIdx.x, &mbar, smem_raw)) return;
-  line_fft_body<LOGL, C, true, KIND, false, false, 0, true>(p, blockIdx.x);
+  line_fft_body<LOGL, C, true, KIND, TSTORE, false, 0, true>(p, blockIdx.x);
 }
 
 // One launch of a multi-transform queue: a device-side table of segments
@@ -1481,6 +1485,7 @@ line_fft_tma(const LineParams p, const __grid_constant__ TmaTile tm) {
 struct Segment {
   LineParams p;
   long long cta0;
+  const TmaTile* tma;   // TMA-capable kernels: this segment's tensor maps (global memory), or null
 };
 
 __device__ __forceinline__ void stage_params(LineParams& dst, const LineParams& src) {
@@ -1492,10 +1497,26 @@ __device__ __forceinline__ void stage_params(LineParams& dst, const LineParams& 
   }
 }
 
-template <int LOGL, int C, bool COLS, int KIND, bool TSTORE, bool TC = false, int UNIT = 0>
+// TMA: every segment has tensor maps and loads its tiles by TMA (as
+// line_fft_tma); segments without them go to the LSU form of the kernel.
+template <int LOGL, int C, bool COLS, int KIND, bool TSTORE, bool TC = false, int UNIT = 0, bool TMA = false>
 __global__ void __launch_bounds__(Sched<LOGL>::T * C, min_ctas<Sched<LOGL>::T * C>())
 line_fft_grouped(const Segment* __restrict__ segs, const int* __restrict__ seg_of, long long total) {
   __shared__ LineParams sp;
+  if constexpr (TMA) {
+    static_assert(COLS && !TC && UNIT == 0, "TMA tiles: cols passes over split planes");
+    __shared__ __align__(8) uint64_t mbar;
+    extern __shared__ __align__(1024) float2 smem_raw[];
+    for (long long v = blockIdx.x; v < total; v += gridDim.x) {
+      const int sg = __ldg(seg_of + v);
+      __syncthreads();
+      stage_params(sp, segs[sg].p);
+      __syncthreads();
+      if (!tma_load_tile<C>(sp, *segs[sg].tma, v - segs[sg].cta0, &mbar, smem_raw)) return;
+      line_fft_body<LOGL, C, true, KIND, TSTORE, false, 0, true>(sp, v - segs[sg].cta0);
+    }
+    return;
+  }
   if constexpr (TC) {
     __shared__ __align__(1024) unsigned char bt[4096];
     __shared__ __align__(8) uint64_t mbar;

@@ -365,6 +365,10 @@ static View inter_view(int b, long long off = 0) {  // re,im pairs in one array
 #ifndef AFFT_TMA_C2C11
 #define AFFT_TMA_C2C11 0
 #endif
+// ... and of the transposing-store passes (four-step pass A)
+#ifndef AFFT_TMA_TSTORE
+#define AFFT_TMA_TSTORE 1
+#endif
 #ifndef AFFT_TMA_R2C11
 #define AFFT_TMA_R2C11 0
 #endif
@@ -458,17 +462,25 @@ struct Builder {
     }
     // cols passes over split planes: the variant with TMA-loaded input tiles
     // (taken at launch when the bound arrays meet its alignment rules)
-    if (AFFT_COLS_TMA && !f64 && !tc && cols && !tstore && !cpairs && !tune.cols_lsu &&
-        (kind == LK_C2C || kind == LK_R2C || kind == LK_C2R)) {
+    if (AFFT_COLS_TMA && !f64 && !tc && cols && !cpairs && !tune.cols_lsu &&
+        (kind == LK_C2C || kind == LK_R2C || kind == LK_C2R) && (!tstore || kind == LK_C2C)) {
       LineKernel kt;
       // (the 2048-point R2C pass: unsplit, one CTA per tile, replacing the
       // split form; its LSU kernel is the fallback)
       // (kernels compare by shape: each translation unit has its own host
       // stub of a template kernel, so their addresses differ)
       const bool want = logl < 11 || (kind == LK_C2C ? AFFT_TMA_C2C11 : kind == LK_R2C ? AFFT_TMA_R2C11 : AFFT_TMA_C2R11);
-      if (want && get_cols_tma(logl, kind, &kt) && kt.kind == op.k.kind && kt.logl == op.k.logl &&
-          kt.unit == op.k.unit && !op.k.tstore && !op.k.tc)
+      const bool have = tstore ? AFFT_TMA_TSTORE && get_cols_tma_tstore(logl, &kt) : get_cols_tma(logl, kind, &kt);
+      if (want && have && kt.kind == op.k.kind && kt.logl == op.k.logl && kt.unit == op.k.unit &&
+          kt.tstore == op.k.tstore && !op.k.tc)
         op.k = kt;
+    }
+    // another tile width for 256- and 512-point complex cols passes, when tuned so
+    LineKernel ka;
+    if (tune.cols_c && !f64 && !tc && cols && !tstore && !cpairs && kind == LK_C2C &&
+        get_cols_c2c_alt(logl, tune.cols_c, &ka)) {
+      op.k = ka;
+      if (!AFFT_COLS_TMA || tune.cols_lsu) op.k.tma = nullptr, op.k.grouped_tma = nullptr;
     }
     op.in = in;
     op.out = out;
@@ -679,9 +691,12 @@ std::unique_ptr<Plan> build_plan(int kind, int ndim, const long long* dims, long
   View src = inter ? inter_view(B_SRC_RE) : split_view(B_SRC_RE, B_SRC_IM);
   View dst = inter ? inter_view(B_DST_RE) : split_view(B_DST_RE, B_DST_IM);
 
+  Tuning tn;
+  if (tune) tn = *tune;
+  else if (!dry && form == 0) tn = tuned_choice(kind, ndim, dims, batch, format);
+  if (tn.tc && form == 0) P->form = form = FORM_TC;   // tuned to the tensor-core form
   Builder b(*P, dry);
-  if (tune) b.tune = *tune;
-  else if (!dry && form == 0) b.tune = tuned_choice(kind, ndim, dims, batch, format);
+  b.tune = tn;
   if (kind == K_C || kind == K_CI) {
     P->in_elems = N;
     P->out_elems = N;

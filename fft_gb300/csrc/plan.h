@@ -96,15 +96,22 @@ struct Plan {
 // built-in four-step split of long axes, 1 the other half first; real_inv:
 // 0 the fused paired pre-pass for long 1D real inverses where it applies,
 // 1 the standalone pre-pass; cols_lsu: 0 TMA-loaded input tiles for the
-// cols passes that have them, 1 the LSU loads.
+// cols passes that have them, 1 the LSU loads; tc: 1 the tensor-core form
+// (plans of the plain form only); cols_c: 8 or 32 lines per CTA for
+// 256-point, 16 for 512-point complex cols passes instead of the default.
 struct Tuning {
   int split = 0;
   int real_inv = 0;
   int cols_lsu = 0;   // 1: cols passes load their tiles through the LSU even where TMA applies
+  int tc = 0;         // 1: the split-precision tensor-core form where a pass has one
+  int cols_c = 0;     // lines per CTA of the 256- and 512-point complex cols passes (0: the default)
 };
 // The tuned choice for a shape on the current device, if the autotuner has
 // one (tuning it first when AFFT_GB300_AUTOTUNE=1); else the defaults.
 Tuning tuned_choice(int kind, int ndim, const long long* dims, long long batch, int format);
+// The tuned choice for a queue's transforms of one shape (split format),
+// tuning it first (at a batch of about 2^24 elements) when none is known.
+Tuning tuned_for_queue(int kind, int ndim, const long long* dims);
 
 // Build a plan; returns nullptr and sets the error on failure.
 // dry: build the op list only (no device calls, twiddle pointers null), for

@@ -46,10 +46,13 @@ struct Group {
 
 struct QueueImpl {
   int form = 0;
+  bool tuned = false;   // plans take the autotuner's per-shape queue choices
   std::vector<afft_gb300_desc> descs;
   std::map<std::vector<long long>, std::shared_ptr<Plan>> plans;
   std::vector<Group> groups;
   float* arena = nullptr;
+  std::vector<TmaTile> tma_host;   // tensor maps of the TMA-fed segments
+  TmaTile* d_tma = nullptr;
   cudaGraphExec_t exec = nullptr;
   cudaStream_t stream = nullptr;
   int device = 0;
@@ -60,6 +63,7 @@ struct QueueImpl {
       if (g.d_map) cudaFree(g.d_map);
     }
     if (arena) cudaFree(arena);
+    if (d_tma) cudaFree(d_tma);
     if (stream) cudaStreamDestroy(stream);
   }
 };
@@ -74,6 +78,13 @@ static LineIO bind_io(const IOSpec& s, float* const* base) {
   o.qshift = s.qshift;
   o.qmask = s.qmask;
   return o;
+}
+
+static LineParams bind_line_params(const Op& op, float* const* base) {
+  LineParams p = op.p;
+  p.in = bind_io(op.in, base);
+  p.out = bind_io(op.out, base);
+  return p;
 }
 
 static int build_queue(QueueImpl& Q) {
@@ -99,7 +110,9 @@ static int build_queue(QueueImpl& Q) {
     key.insert(key.end(), dims, dims + nd);
     auto it = Q.plans.find(key);
     if (it == Q.plans.end()) {
-      auto P = build_plan(d.kind, nd, dims, 1, 0, false, Q.form);
+      Tuning tq;
+      if (Q.tuned) tq = tuned_for_queue(d.kind, nd, dims);
+      auto P = build_plan(d.kind, nd, dims, 1, 0, false, Q.form, Q.tuned ? &tq : nullptr);
       if (!P) return AFFT_GB300_EINVAL;
       it = Q.plans.emplace(key, std::shared_ptr<Plan>(P.release())).first;
     }
@@ -126,7 +139,12 @@ static int build_queue(QueueImpl& Q) {
         set_error(AFFT_GB300_ECUDA, "plan is missing a twiddle table");
         return AFFT_GB300_ECUDA;
       }
-      const void* kid = op.type == OP_LINE ? (const void*)op.k.grouped : (const void*)&elementwise_grouped;
+      // a TMA-capable pass whose tensor maps encode for this transform's
+      // arrays goes to the TMA form of the grouped kernel
+      TmaTile tm;
+      const bool tma = op.type == OP_LINE && op.k.grouped_tma && tma_tile(bind_line_params(op, base), op.k, &tm);
+      const void* kid = op.type != OP_LINE ? (const void*)&elementwise_grouped
+                                           : (tma ? (const void*)op.k.grouped_tma : (const void*)op.k.grouped);
       auto key = std::make_pair((int)i, kid);
       auto it = gidx.find(key);
       if (it == gidx.end()) {
@@ -135,6 +153,7 @@ static int build_queue(QueueImpl& Q) {
         g.id = (int)Q.groups.size();
         g.line = op.type == OP_LINE;
         g.k = op.k;
+        if (tma) g.k.grouped = op.k.grouped_tma;
         it = gidx.emplace(key, Q.groups.size()).first;
         Q.groups.push_back(g);
       }
@@ -147,6 +166,13 @@ static int build_queue(QueueImpl& Q) {
         s.p.in = bind_io(op.in, base);
         s.p.out = bind_io(op.out, base);
         s.cta0 = op.grid;  // for now the segment's CTA count
+        // the tensor maps of a TMA-fed segment (the pointers are fixed now);
+        // s.tma holds 1 + the map's index until the map array exists
+        s.tma = nullptr;
+        if (tma) {
+          Q.tma_host.push_back(tm);
+          s.tma = reinterpret_cast<const TmaTile*>((uintptr_t)Q.tma_host.size());
+        }
         g.segs.push_back(s);
       } else {
         EwSegment s{};
@@ -165,6 +191,17 @@ static int build_queue(QueueImpl& Q) {
       }
     }
   }
+  if (!Q.tma_host.empty() &&
+      (cudaMalloc(&Q.d_tma, Q.tma_host.size() * sizeof(TmaTile)) != cudaSuccess ||
+       cudaMemcpy(Q.d_tma, Q.tma_host.data(), Q.tma_host.size() * sizeof(TmaTile), cudaMemcpyHostToDevice) !=
+           cudaSuccess)) {
+    cudaGetLastError();
+    set_error(AFFT_GB300_ENOMEM, "queue tensor-map upload failed");
+    return AFFT_GB300_ENOMEM;
+  }
+  for (auto& g : Q.groups)
+    for (auto& s : g.segs)
+      if (s.tma) s.tma = Q.d_tma + ((uintptr_t)s.tma - 1);
   // largest segments first, prefix sums, device tables, launch shapes
   for (auto& g : Q.groups) {
     void* host = nullptr;
@@ -300,13 +337,14 @@ afft_gb300_queue* afft_gb300_queue_create_ex(const afft_gb300_desc* descs, size_
     set_error(AFFT_GB300_EINVAL, "null descriptor array");
     return nullptr;
   }
-  if (flags & ~FORM_TC) {   // FP32 data only (FP64 transforms have no grouped kernels)
-    set_error(AFFT_GB300_EINVAL, "queue flags: 0 or AFFT_GB300_FORM_TC");
+  if (flags & ~(FORM_TC | AFFT_GB300_QUEUE_TUNED)) {   // FP32 data only (FP64 transforms have no grouped kernels)
+    set_error(AFFT_GB300_EINVAL, "queue flags: AFFT_GB300_FORM_TC and/or AFFT_GB300_QUEUE_TUNED");
     return nullptr;
   }
   auto* q = new afft_gb300_queue();
   QueueImpl& Q = q->impl;
   Q.form = flags & FORM_TC;
+  Q.tuned = (flags & AFFT_GB300_QUEUE_TUNED) != 0;
   cudaGetDevice(&Q.device);
   Q.descs.assign(descs, descs + count);
   if (cudaStreamCreateWithFlags(&Q.stream, cudaStreamNonBlocking) != cudaSuccess) {

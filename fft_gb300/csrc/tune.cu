@@ -1,16 +1,25 @@
 // Autotuner: per (device, kind, dims, batch, format), time the plan variants
 // the shape allows and keep the fastest for later plans.
 //
-// The variants (Tuning in plan.h) are choices the fixed heuristics make
-// otherwise: the four-step split of axes too long for one CTA (which half the
-// first pass takes), and for long 1D real inverses whether the real pre-pass
-// rides in the first four-step pass (over mirrored column pairs) or runs
-// standalone.  Each distinct variant is built as a device plan and timed with
-// CUDA events on zeroed scratch buffers of the current device (2 warm-up and
-// 5 timed launches, median).  Choices live in a process-wide table and, when
-// AFFT_GB300_TUNE_CACHE names a file, in that file (one entry per line,
-// loaded on first use, rewritten after each tuning).  AFFT_GB300_AUTOTUNE=1
-// tunes every new shape when its first plan is built.
+// The variants (Tuning in plan.h) are choices the fixed rules make
+// otherwise:
+//  - the four-step split of axes too long for one CTA (which half the first
+//    pass takes);
+//  - for long 1D real inverses, the real pre-pass riding in the first
+//    four-step pass (over mirrored column pairs) or standalone;
+//  - cols passes loading their input tiles by TMA or through the LSU;
+//  - the tile width (lines per CTA) of 256- and 512-point complex cols passes;
+//  - the plain FP32 form or the split-precision tensor-core form of the
+//    passes that have one.
+// Each distinct variant (distinct kernels or launch shapes) is built as a
+// device plan and timed with CUDA events on zeroed buffers of the current
+// device (2 warm-up and 5 timed launches, median).  Choices live in a
+// process-wide table and, when AFFT_GB300_TUNE_CACHE names a file, in that
+// file (one entry per line, loaded on first use, rewritten after each
+// tuning).  AFFT_GB300_AUTOTUNE=1 tunes every new shape when its first plan
+// is built.  Queues created with AFFT_GB300_QUEUE_TUNED tune each distinct
+// shape of their transforms at a batch of about 2^24 elements and keep the
+// choice under batch 0 (the queue's entry for that shape).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -69,7 +78,8 @@ std::string key_of(int kind, int ndim, const long long* dims, long long batch, i
 }
 
 // file format: a JSON object, one entry per line:
-//   "<key>": {"split": S, "real_inv": R, "ms": T},
+//   "<key>": {"split": S, "real_inv": R, "cols_lsu": U, "tc": T, "cols_c": C, "ms": M},
+// (entries of the older form, without cols_lsu / tc / cols_c, still load)
 void load_locked(TuneCache& C) {
   if (C.loaded) return;
   C.loaded = true;
@@ -85,8 +95,11 @@ void load_locked(TuneCache& C) {
     char* b = std::strchr(a + 1, '"');
     if (!b) continue;
     Entry e;
-    if (std::sscanf(b + 1, " : {\"split\": %d, \"real_inv\": %d, \"ms\": %lf", &e.t.split, &e.t.real_inv, &e.ms) ==
-        3)
+    if (std::sscanf(b + 1,
+                    " : {\"split\": %d, \"real_inv\": %d, \"cols_lsu\": %d, \"tc\": %d, \"cols_c\": %d, \"ms\": %lf",
+                    &e.t.split, &e.t.real_inv, &e.t.cols_lsu, &e.t.tc, &e.t.cols_c, &e.ms) == 6 ||
+        std::sscanf(b + 1, " : {\"split\": %d, \"real_inv\": %d, \"ms\": %lf", &e.t.split, &e.t.real_inv, &e.ms) ==
+            3)
       C.table[std::string(a + 1, b)] = e;
   }
   std::fclose(f);
@@ -100,8 +113,10 @@ void save_locked(const TuneCache& C) {
   std::fprintf(f, "{\n");
   size_t i = 0;
   for (const auto& kv : C.table) {
-    std::fprintf(f, "\"%s\": {\"split\": %d, \"real_inv\": %d, \"ms\": %.6f}%s\n", kv.first.c_str(), kv.second.t.split,
-                 kv.second.t.real_inv, kv.second.ms, ++i < C.table.size() ? "," : "");
+    const Tuning& t = kv.second.t;
+    std::fprintf(f, "\"%s\": {\"split\": %d, \"real_inv\": %d, \"cols_lsu\": %d, \"tc\": %d, \"cols_c\": %d, \"ms\": %.6f}%s\n",
+                 kv.first.c_str(), t.split, t.real_inv, t.cols_lsu, t.tc, t.cols_c, kv.second.ms,
+                 ++i < C.table.size() ? "," : "");
   }
   std::fprintf(f, "}\n");
   std::fclose(f);
@@ -113,8 +128,9 @@ std::string signature(const Plan& P) {
   std::string s;
   char buf[128];
   for (const Op& op : P.ops) {
-    snprintf(buf, sizeof buf, "%d:%p:%d:%lld;", op.type, op.type == OP_LINE ? (const void*)op.k.fn : nullptr,
-             op.k.logl, op.type == OP_LINE ? op.p.nlines : op.rp.nlines);
+    snprintf(buf, sizeof buf, "%d:%p:%p:%d:%d:%d:%lld;", op.type, op.type == OP_LINE ? (const void*)op.k.fn : nullptr,
+             op.type == OP_LINE ? (const void*)op.k.tma : nullptr, op.k.logl, op.k.lines_per_cta, op.k.tc,
+             op.type == OP_LINE ? op.p.nlines : op.rp.nlines);
     s += buf;
   }
   return s;
@@ -162,21 +178,30 @@ int tune_shape(int kind, int ndim, const long long* dims, long long batch, int f
   } reset;
   std::vector<std::pair<Tuning, std::unique_ptr<Plan>>> cands;
   std::vector<std::string> sigs;
+  static const int widths[] = {0, 8, 16, 32};
   for (int split = 0; split < 2; split++)
-    for (int real_inv = 0; real_inv < 2; real_inv++) {
-      Tuning t;
-      t.split = split;
-      t.real_inv = real_inv;
-      auto P = build_plan(kind, ndim, dims, batch, format, false, 0, &t);
-      if (!P) {
-        clear_error();
-        continue;
-      }
-      std::string sg = signature(*P);
-      if (std::find(sigs.begin(), sigs.end(), sg) != sigs.end()) continue;
-      sigs.push_back(sg);
-      cands.emplace_back(t, std::move(P));
-    }
+    for (int real_inv = 0; real_inv < 2; real_inv++)
+      for (int lsu = 0; lsu < 2; lsu++)
+        for (int tc = 0; tc < 2; tc++)
+          for (int w : widths) {
+            Tuning t;
+            t.split = split;
+            t.real_inv = real_inv;
+            t.cols_lsu = lsu;
+            t.tc = tc;
+            t.cols_c = w;
+            auto P = build_plan(kind, ndim, dims, batch, format, false, 0, &t);
+            if (!P) {
+              clear_error();
+              continue;
+            }
+            // variants that build the same launches are one candidate (the
+            // first, i.e. the most default, represents them)
+            std::string sg = signature(*P);
+            if (std::find(sigs.begin(), sigs.end(), sg) != sigs.end()) continue;
+            sigs.push_back(sg);
+            cands.emplace_back(t, std::move(P));
+          }
   if (cands.empty()) {
     set_error(AFFT_GB300_EINVAL, "no plan for this shape");
     return AFFT_GB300_EINVAL;
@@ -210,15 +235,20 @@ int tune_shape(int kind, int ndim, const long long* dims, long long batch, int f
   out->t = cands[best].first;
   out->ms = times[best];
   if (report) {
-    char buf[160];
+    char buf[256];
     *report = "{\"key\":\"" + key_of(kind, ndim, dims, batch, format) + "\",\"candidates\":[";
     for (size_t i = 0; i < cands.size(); i++) {
-      snprintf(buf, sizeof buf, "%s{\"split\":%d,\"real_inv\":%d,\"launches\":%zu,\"ms\":%.6f}", i ? "," : "",
-               cands[i].first.split, cands[i].first.real_inv, cands[i].second->ops.size(), times[i]);
+      const Tuning& t = cands[i].first;
+      snprintf(buf, sizeof buf,
+               "%s{\"split\":%d,\"real_inv\":%d,\"cols_lsu\":%d,\"tc\":%d,\"cols_c\":%d,\"launches\":%zu,"
+               "\"ms\":%.6f}",
+               i ? "," : "", t.split, t.real_inv, t.cols_lsu, t.tc, t.cols_c, cands[i].second->ops.size(), times[i]);
       *report += buf;
     }
-    snprintf(buf, sizeof buf, "],\"chosen\":{\"split\":%d,\"real_inv\":%d,\"ms\":%.6f}}", out->t.split,
-             out->t.real_inv, out->ms);
+    const Tuning& t = out->t;
+    snprintf(buf, sizeof buf,
+             "],\"chosen\":{\"split\":%d,\"real_inv\":%d,\"cols_lsu\":%d,\"tc\":%d,\"cols_c\":%d,\"ms\":%.6f}}",
+             t.split, t.real_inv, t.cols_lsu, t.tc, t.cols_c, out->ms);
     *report += buf;
   }
   return 0;
@@ -245,6 +275,26 @@ Tuning tuned_choice(int kind, int ndim, const long long* dims, long long batch, 
     clear_error();
   }
   return Tuning();
+}
+
+Tuning tuned_for_queue(int kind, int ndim, const long long* dims) {
+  auto& C = cache();
+  std::lock_guard<std::mutex> g(C.mu);
+  load_locked(C);
+  const std::string key = key_of(kind, ndim, dims, 0, afft_split);
+  auto it = C.table.find(key);
+  if (it != C.table.end()) return it->second.t;
+  long long n = 1;
+  for (int i = 0; i < ndim; i++) n *= dims[i];
+  const long long batch = std::max(1LL, (1LL << 24) / n);
+  Entry e;
+  if (tune_shape(kind, ndim, dims, batch, afft_split, &e, nullptr) != 0) {
+    clear_error();
+    return Tuning();
+  }
+  C.table[key] = e;
+  save_locked(C);
+  return e.t;
 }
 
 }  // namespace agb

@@ -227,10 +227,13 @@ AFFT_GB300_API size_t afft_gb300_plan_describe(int kind, size_t ndim,
 
 /* Autotuner (no counterpart in afft): times the plan variants a shape allows
  * on the current device and keeps the fastest for later plans of the same
- * (device, kind, dims, batch, format).  The variants are the four-step split
- * of axes longer than one CTA holds (which half the first pass takes) and,
- * for long 1D real inverses, the real pre-pass fused into the first pass or
- * run on its own.  It allocates scratch device buffers for the timing.
+ * (device, kind, dims, batch, format).  The variants: the four-step split
+ * of axes longer than one CTA holds (which half the first pass takes); for
+ * long 1D real inverses, the real pre-pass fused into the first pass or run
+ * on its own; cols passes loading their tiles by TMA or through the LSU;
+ * 8, 16 or 32 lines per CTA for 256- and 512-point complex cols passes; and
+ * the plain FP32 or the split-precision tensor-core form of the passes that
+ * have one.  It allocates scratch device buffers for the timing.
  * Choices are kept for the process and, when the environment variable
  * AFFT_GB300_TUNE_CACHE names a file, stored there and reloaded on first use;
  * with AFFT_GB300_AUTOTUNE=1 every new shape is tuned when its first plan is
@@ -294,7 +297,15 @@ typedef struct afft_gb300_desc
 typedef struct afft_gb300_queue afft_gb300_queue;
 AFFT_GB300_API afft_gb300_queue* afft_gb300_queue_create(const afft_gb300_desc* descs,
   size_t count);
-/* As afft_gb300_queue_create; flags: 0 or AFFT_GB300_FORM_TC. */
+/* Queue flag (no counterpart in afft): every distinct (kind, shape) among
+ * the queue's transforms takes the autotuner's choice for queues -- tuned
+ * on first use at a batch of about 2^24 elements, timed on this device, and
+ * kept like afft_gb300_tune's choices (under batch 0) -- instead of the
+ * built-in defaults.  Tuning allocates device buffers while the queue is
+ * created. */
+enum { AFFT_GB300_QUEUE_TUNED = 0x400 };
+/* As afft_gb300_queue_create; flags: 0, AFFT_GB300_FORM_TC and/or
+ * AFFT_GB300_QUEUE_TUNED. */
 AFFT_GB300_API afft_gb300_queue* afft_gb300_queue_create_ex(
   const afft_gb300_desc* descs, size_t count, int flags);
 /* `stream` as for afft_gb300_transform_async (NULL = default stream). */

@@ -1,7 +1,9 @@
 """GPU tests of the autotuner (afft_gb300_tune): it times the plan variants a
-shape allows, keeps the fastest for later plans of that shape, and persists
-choices in the file named by AFFT_GB300_TUNE_CACHE; plans built from a tuned
-choice must still agree with the FP64 oracle."""
+shape allows (four-step split, fused or standalone real pre-pass, TMA or LSU
+tile loads, cols tile width, plain or tensor-core form), keeps the fastest
+for later plans of that shape, and persists choices in the file named by
+AFFT_GB300_TUNE_CACHE; plans built from any variant must still agree with
+the FP64 oracle, and so must a queue built from tuned per-shape choices."""
 import json
 import os
 import subprocess
@@ -62,8 +64,70 @@ def test_tune_picks_the_fastest_and_plans_stay_correct(kind, dims, batch, dev):
 
 
 def test_tune_shape_without_choices(dev):
-    rep = G.tune("c", [4096], 64)
+    rep = G.tune("c", [1024], 64)
     assert len(rep["candidates"]) == 1 and rep["chosen"]["ms"] < 0
+
+
+def test_tune_weighs_tile_loads_widths_and_form(dev):
+    # 256-point cols passes: TMA or LSU loads, 8/16/32-line tiles, and the
+    # tensor-core form; every distinct variant is timed
+    rep = G.tune("c", [256, 256, 16], 2)
+    cands = rep["candidates"]
+    seen = {(c["cols_lsu"], c["cols_c"], c["tc"]) for c in cands}
+    assert {(0, 0, 0), (1, 0, 0), (0, 8, 0), (0, 32, 0)} <= seen, rep
+    assert any(c["tc"] for c in cands), rep
+    timed = [c for c in cands if c["ms"] > 0]
+    assert rep["chosen"]["ms"] == min(c["ms"] for c in timed)
+    batched_parity("c", [256, 256, 16], 2)
+
+
+# variants forced through the cache file: the key holds the batch, so each
+# batch of one shape can take another variant in one process
+VARIANTS = [dict(split=0, real_inv=0, cols_lsu=l, tc=t, cols_c=w)
+            for l in (0, 1) for t in (0, 1) for w in (0, 8, 32)]
+
+
+def test_every_tile_and_form_variant_is_correct(tmp_path, dev):
+    name = torch.cuda.get_device_name(0).replace(" ", "_")
+    path = str(tmp_path / "tune_variants.json")
+    lines = []
+    for i, v in enumerate(VARIANTS):
+        for kind, code in (("c", 0), ("ci", 1)):
+            lines.append("\"%s|%d|256x256x8|%d|0\": {\"split\": 0, \"real_inv\": 0, \"cols_lsu\": %d, \"tc\": %d, "
+                         "\"cols_c\": %d, \"ms\": 1.0}" % (name, code, i + 1, v["cols_lsu"], v["tc"], v["cols_c"]))
+        lines.append("\"%s|0|512x512|%d|0\": {\"split\": 0, \"real_inv\": 0, \"cols_lsu\": %d, \"tc\": %d, "
+                     "\"cols_c\": %d, \"ms\": 1.0}" % (name, i + 1, v["cols_lsu"], v["tc"], 16 if v["cols_c"] else 0))
+    with open(path, "w") as f:
+        f.write("{\n" + ",\n".join(lines) + "\n}\n")
+    code = ("import sys; sys.path.insert(0, %r); sys.path.insert(0, %r)\n"
+            "import test_tune_gpu as T\n"
+            "for b in range(1, %d):\n"
+            "    T.batched_parity('c', [256, 256, 8], b)\n"
+            "    T.batched_parity('ci', [256, 256, 8], b)\n"
+            "    T.batched_parity('c', [512, 512], b)\n" % (ROOT, os.path.join(ROOT, "tests"), len(VARIANTS) + 1))
+    env = dict(os.environ, AFFT_GB300_TUNE_CACHE=path)
+    r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stderr[-2000:]
+
+
+def test_tuned_queue_matches_fp64(tmp_path, dev):
+    # a queue whose plans take the per-shape queue choices (tuned on first
+    # use) against the FP64 oracle, transform by transform
+    from fft_gb300 import uneven as U
+    code = ("import sys; sys.path.insert(0, %r); sys.path.insert(0, %r)\n"
+            "import torch, fft_gb300 as G\nfrom fft_gb300 import uneven as U\n"
+            "import test_queue_gpu as Q\n"
+            "items = U.uneven_batch(10000, seed=5)[:120]\n"
+            "buf, offs = U.allocate(items, torch.device('cuda:0'), seed=6)\n"
+            "q = G.Queue(U.descs(items, buf, offs), tuned=True)\n"
+            "q.run(); torch.cuda.synchronize()\n"
+            "print('worst %%.2e' %% Q._check_all(items, buf, offs))\n" % (ROOT, os.path.join(ROOT, "tests")))
+    env = dict(os.environ, AFFT_GB300_TUNE_CACHE=str(tmp_path / "queue_tune.json"))
+    r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stderr[-3000:]
+    text = open(str(tmp_path / "queue_tune.json")).read()
+    assert "|0|0\"" in text          # entries kept under batch 0 (the queue's)
+    json.loads(text)
 
 
 def test_every_variant_is_correct(tmp_path, dev):
