@@ -69,6 +69,10 @@ bool get_cols_tma(int logl, int kind, LineKernel* out);
 // the transposing-store complex cols passes (four-step pass A) of 2^8 ..
 // 2^10 points with TMA-loaded input tiles (k_cols_tma_ts.cu)
 bool get_cols_tma_tstore(int logl, LineKernel* out);
+// complex cols passes over interleaved input pairs (pairs bit 0 set: 1 or
+// 3), plain or with the transposing store, 2^8 and 2^9 points, with TMA
+// loads of the interleaved tile (k_cols_tma_pairs.cu)
+bool get_cols_tma_pairs(int logl, bool tstore, int pairs, LineKernel* out);
 
 // cols c2c passes (not transposing) with another tile width, for the
 // autotuner: 256 points in 8 or 32 lines, 512 points in 16; TMA-fed
@@ -144,16 +148,16 @@ LineKernel make_line_kernel() {
 }
 
 // a cols pass with its TMA-fed variant (CC: lines per CTA, 0 = the default)
-template <int LOGL, int KIND, int CC = 0, bool TSTORE = false>
+template <int LOGL, int KIND, int CC = 0, bool TSTORE = false, int UNIT = 0>
 LineKernel make_tma_kernel() {
   constexpr int C = CC ? CC : lines_per_cta_k<LOGL, true, KIND>();
   static_assert((size_t)LineSmem<LOGL, C, true, TSTORE, false>::FLOAT2S * sizeof(float2) >=
                     (size_t)2 * (1 << LOGL) * C * sizeof(float),
                 "the input tile fits the exchange buffer it aliases");
   static_assert(C * sizeof(float) % 16 == 0, "tile columns span whole 16-byte units");
-  LineKernel k = make_line_kernel<LOGL, true, KIND, TSTORE, false, 0, C>();
-  k.tma = &line_fft_tma<LOGL, C, KIND, TSTORE>;
-  k.grouped_tma = &line_fft_grouped<LOGL, C, true, KIND, TSTORE, false, 0, true>;
+  LineKernel k = make_line_kernel<LOGL, true, KIND, TSTORE, false, UNIT, C>();
+  k.tma = &line_fft_tma<LOGL, C, KIND, TSTORE, UNIT>;
+  k.grouped_tma = &line_fft_grouped<LOGL, C, true, KIND, TSTORE, false, UNIT, true>;
   return k;
 }
 

@@ -894,8 +894,8 @@ __device__ __forceinline__ void rows_stage_out_reals(const LineParams& p, long l
 // floats; C2R tiles hold bins 0 .. L-1 there and read bin L directly.
 template <int LOGL, int C, bool COLS, int KIND, bool TSTORE, bool TC = false, int UNIT = 0, bool TMA = false>
 __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta, TcState* ts = nullptr) {
-  static_assert(!TMA || (COLS && !TC && UNIT == 0 && (!TSTORE || KIND == LK_C2C)),
-                "TMA tiles: cols passes over split planes");
+  static_assert(!TMA || (COLS && !TC && (UNIT == 0 || KIND == LK_C2C) && (!TSTORE || KIND == LK_C2C)),
+                "TMA tiles: cols passes");
   if constexpr (KIND == LK_R2C_HALF) {
     static_assert(COLS && !TSTORE && !TC, "the split R2C pass is a plain cols pass");
     r2c_half_body<LOGL, C>(p, cta);
@@ -1022,13 +1022,21 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
       }
     }
     if constexpr (TMA) {
-      // element i of column c at raw[i C + c] (re plane), raw[L C + i C + c]
-      // (im plane): a warp's 32 lanes read 32 consecutive words
-      const float* raw = reinterpret_cast<const float*>(smem_raw);
+      if constexpr (CPAIRS & 1) {
+        // input pairs: element i of column c is the pair raw2[i C + c]; a
+        // warp's lanes read 32 consecutive pairs
+        const float2* raw2 = reinterpret_cast<const float2*>(smem_raw);
 #pragma unroll
-      for (int e = 0; e < E; e++) {
-        const int i = t + T * e;
-        v[e] = make_float2(raw[i * C + c], raw[L * C + i * C + c]);
+        for (int e = 0; e < E; e++) v[e] = raw2[(t + T * e) * C + c];
+      } else {
+        // element i of column c at raw[i C + c] (re plane), raw[L C + i C + c]
+        // (im plane): a warp's 32 lanes read 32 consecutive words
+        const float* raw = reinterpret_cast<const float*>(smem_raw);
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+          const int i = t + T * e;
+          v[e] = make_float2(raw[i * C + c], raw[L * C + i * C + c]);
+        }
       }
       if (p.inverse) {
 #pragma unroll
@@ -1412,9 +1420,10 @@ line_fft(const LineParams p) {
 // hi * 4 are multiples of 16 bytes and the column of a tile is a multiple of
 // C (>= 4 floats), so every box starts on a 16-byte boundary.
 struct TmaTile {
-  CUtensorMap re, im;   // the input's re and im planes
+  CUtensorMap re, im;   // the input's re and im planes (pairs: re maps the interleaved array, im unused)
   int box_rows;         // rows per box (<= 256, divides L)
   int rows;             // rows loaded per plane (L)
+  int pairs;            // 1: one interleaved array of re,im pairs, boxes of 2 C floats
 };
 
 __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int x, int y, int z,
@@ -1446,10 +1455,16 @@ __device__ __forceinline__ bool tma_load_tile(const LineParams& p, const TmaTile
     const uint32_t bytes = 2u * (uint32_t)tm.rows * C * 4u;
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(bytes) : "memory");
     const uint32_t d = smem_u32(dst);
-    const uint32_t plane = (uint32_t)tm.rows * C * 4u;
-    for (int r = 0; r < tm.rows; r += tm.box_rows) {
-      tma_load_3d(d + (uint32_t)r * C * 4u, &tm.re, col, r, outer, mb);
-      tma_load_3d(d + plane + (uint32_t)r * C * 4u, &tm.im, col, r, outer, mb);
+    if (tm.pairs) {
+      // one array of pairs: the tile is [rows][2 C floats], column col at float 2 col
+      for (int r = 0; r < tm.rows; r += tm.box_rows)
+        tma_load_3d(d + (uint32_t)r * C * 8u, &tm.re, 2 * col, r, outer, mb);
+    } else {
+      const uint32_t plane = (uint32_t)tm.rows * C * 4u;
+      for (int r = 0; r < tm.rows; r += tm.box_rows) {
+        tma_load_3d(d + (uint32_t)r * C * 4u, &tm.re, col, r, outer, mb);
+        tma_load_3d(d + plane + (uint32_t)r * C * 4u, &tm.im, col, r, outer, mb);
+      }
     }
   }
   const bool ok = __syncthreads_and(tc_wait(mb, 0));
@@ -1466,13 +1481,13 @@ __device__ __forceinline__ bool tma_load_tile(const LineParams& p, const TmaTile
   return ok;
 }
 
-template <int LOGL, int C, int KIND, bool TSTORE = false>
+template <int LOGL, int C, int KIND, bool TSTORE = false, int UNIT = 0>
 __global__ void __launch_bounds__(Sched<LOGL>::T * C, min_ctas<Sched<LOGL>::T * C>())
 line_fft_tma(const LineParams p, const __grid_constant__ TmaTile tm) {
   __shared__ __align__(8) uint64_t mbar;
   extern __shared__ __align__(1024) float2 smem_raw[];
   if (!tma_load_tile<C>(p, tm, blockIdx.x, &mbar, smem_raw)) return;
-  line_fft_body<LOGL, C, true, KIND, TSTORE, false, 0, true>(p, blockIdx.x);
+  line_fft_body<LOGL, C, true, KIND, TSTORE, false, UNIT, true>(p, blockIdx.x);
 }
 
 // One launch of a multi-transform queue: a device-side table of segments
@@ -1504,7 +1519,7 @@ __global__ void __launch_bounds__(Sched<LOGL>::T * C, min_ctas<Sched<LOGL>::T * 
 line_fft_grouped(const Segment* __restrict__ segs, const int* __restrict__ seg_of, long long total) {
   __shared__ LineParams sp;
   if constexpr (TMA) {
-    static_assert(COLS && !TC && UNIT == 0, "TMA tiles: cols passes over split planes");
+    static_assert(COLS && !TC, "TMA tiles: cols passes");
     __shared__ __align__(8) uint64_t mbar;
     extern __shared__ __align__(1024) float2 smem_raw[];
     for (long long v = blockIdx.x; v < total; v += gridDim.x) {
@@ -1513,7 +1528,7 @@ line_fft_grouped(const Segment* __restrict__ segs, const int* __restrict__ seg_o
       stage_params(sp, segs[sg].p);
       __syncthreads();
       if (!tma_load_tile<C>(sp, *segs[sg].tma, v - segs[sg].cta0, &mbar, smem_raw)) return;
-      line_fft_body<LOGL, C, true, KIND, TSTORE, false, 0, true>(sp, v - segs[sg].cta0);
+      line_fft_body<LOGL, C, true, KIND, TSTORE, false, UNIT, true>(sp, v - segs[sg].cta0);
     }
     return;
   }

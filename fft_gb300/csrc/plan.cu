@@ -369,6 +369,10 @@ static View inter_view(int b, long long off = 0) {  // re,im pairs in one array
 #ifndef AFFT_TMA_TSTORE
 #define AFFT_TMA_TSTORE 1
 #endif
+// ... and of complex cols passes over interleaved input pairs
+#ifndef AFFT_TMA_PAIRS
+#define AFFT_TMA_PAIRS 1
+#endif
 #ifndef AFFT_TMA_R2C11
 #define AFFT_TMA_R2C11 0
 #endif
@@ -462,15 +466,17 @@ struct Builder {
     }
     // cols passes over split planes: the variant with TMA-loaded input tiles
     // (taken at launch when the bound arrays meet its alignment rules)
-    if (AFFT_COLS_TMA && !f64 && !tc && cols && !cpairs && !tune.cols_lsu &&
-        (kind == LK_C2C || kind == LK_R2C || kind == LK_C2R) && (!tstore || kind == LK_C2C)) {
+    if (AFFT_COLS_TMA && !f64 && !tc && cols && !tune.cols_lsu && (kind == LK_C2C || kind == LK_R2C || kind == LK_C2R) &&
+        (!tstore || kind == LK_C2C) && (cpairs == 0 || (cpairs & 1))) {
       LineKernel kt;
       // (the 2048-point R2C pass: unsplit, one CTA per tile, replacing the
       // split form; its LSU kernel is the fallback)
       // (kernels compare by shape: each translation unit has its own host
       // stub of a template kernel, so their addresses differ)
       const bool want = logl < 11 || (kind == LK_C2C ? AFFT_TMA_C2C11 : kind == LK_R2C ? AFFT_TMA_R2C11 : AFFT_TMA_C2R11);
-      const bool have = tstore ? AFFT_TMA_TSTORE && get_cols_tma_tstore(logl, &kt) : get_cols_tma(logl, kind, &kt);
+      const bool have = (cpairs & 1) ? AFFT_TMA_PAIRS && get_cols_tma_pairs(logl, tstore, cpairs, &kt)
+                        : tstore   ? AFFT_TMA_TSTORE && get_cols_tma_tstore(logl, &kt)
+                                   : get_cols_tma(logl, kind, &kt);
       if (want && have && kt.kind == op.k.kind && kt.logl == op.k.logl && kt.unit == op.k.unit &&
           kt.tstore == op.k.tstore && !op.k.tc)
         op.k = kt;
@@ -953,26 +959,35 @@ bool tma_tile(const LineParams& p, const LineKernel& k, TmaTile* tm) {
   const LineIO& in = p.in;
   const long long L = 1LL << k.logl, C = k.lines_per_cta;
   const long long ncols = in.qmask + 1;
-  if (in.lo != 1 || ncols != (1LL << in.qshift) || ncols % C || p.nlines % ncols || L > (1LL << 16)) return false;
-  if ((reinterpret_cast<uintptr_t>(in.re) | reinterpret_cast<uintptr_t>(in.im)) & 15) return false;
+  // input pairs (cols kernels with pairs bit 0): one interleaved array,
+  // adjacent columns adjacent pairs
+  const bool pairs = (k.unit & 1) != 0;
+  if (in.lo != (pairs ? 2 : 1) || ncols != (1LL << in.qshift) || ncols % C || p.nlines % ncols ||
+      L > (1LL << 16))
+    return false;
+  if (pairs ? (in.im != in.re + 1 || (reinterpret_cast<uintptr_t>(in.re) & 15))
+            : ((reinterpret_cast<uintptr_t>(in.re) | reinterpret_cast<uintptr_t>(in.im)) & 15))
+    return false;
   const long long nouter = p.nlines / ncols;
   const long long rs = in.es * 4, bs = nouter > 1 ? in.hi * 4 : L * in.es * 4;
   if (rs % 16 || bs % 16 || rs <= 0 || bs <= 0 || rs >= (1LL << 40) || bs >= (1LL << 40)) return false;
   auto encode = tensor_map_encoder();
   if (!encode) return false;
-  const cuuint64_t dims[3] = {(cuuint64_t)ncols, (cuuint64_t)L, (cuuint64_t)nouter};
+  const cuuint64_t dims[3] = {(cuuint64_t)(pairs ? 2 * ncols : ncols), (cuuint64_t)L, (cuuint64_t)nouter};
   const cuuint64_t strides[2] = {(cuuint64_t)rs, (cuuint64_t)bs};
   const int br = (int)std::min<long long>(L, 256);
-  const cuuint32_t box[3] = {(cuuint32_t)C, (cuuint32_t)br, 1};
+  const cuuint32_t box[3] = {(cuuint32_t)(pairs ? 2 * C : C), (cuuint32_t)br, 1};
   const cuuint32_t estr[3] = {1, 1, 1};
-  for (int i = 0; i < 2; i++) {
+  for (int i = 0; i < (pairs ? 1 : 2); i++) {
     if (encode(i ? &tm->im : &tm->re, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)(i ? in.im : in.re), dims, strides,
                box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
       return false;
   }
+  if (pairs) tm->im = tm->re;
   tm->box_rows = br;
   tm->rows = (int)L;
+  tm->pairs = pairs ? 1 : 0;
   return true;
 }
 

@@ -1,6 +1,10 @@
 """Run one batched plan on seeded device data a few times, for profiling.
 
     python tests/run_plan.py KIND DIMS BATCH [REPS] [FORM]
+    python tests/run_plan.py queue COUNT [REPS]
+
+The second form runs the first COUNT transforms of the mixed ("uneven")
+batch as one queue (fft_gb300/uneven.py, seed 5) REPS times.
 
 KIND is c, ci, r or ri; DIMS a JSON list such as [256,256,256]; FORM plain
 (default), tc or f64 (double data through the FP64 kernels).  Each
@@ -17,7 +21,21 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 from fft_gb300 import BatchPlan  # noqa: E402
 
 
+def run_queue(count, reps):
+    from fft_gb300 import Queue, uneven as U
+    items = U.uneven_batch(10000, seed=5)[:count]
+    buf, offs = U.allocate(items, torch.device("cuda"))
+    q = Queue(U.descs(items, buf, offs))
+    for _ in range(reps):
+        q.run()
+    torch.cuda.synchronize()
+    print("queue of %d transforms, %d launches per run" % (count, q.launches))
+    return 0
+
+
 def main(argv):
+    if len(argv) >= 2 and argv[0] == "queue":
+        return run_queue(int(argv[1]), int(argv[2]) if len(argv) > 2 else 2)
     if len(argv) < 3:
         print(__doc__)
         return 2
