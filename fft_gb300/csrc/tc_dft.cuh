@@ -56,9 +56,18 @@ __device__ __forceinline__ void tc_commit(uint32_t mbar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar));
 }
 
-// bounded wait on an mbarrier phase; returns false on timeout
-__device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity) {
-  for (int it = 0; it < (1 << 24); it++) {
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Bounded wait on an mbarrier phase: polls until the phase completes or
+// limit_ns of wall time (the %globaltimer clock) has passed, with a poll
+// count cap besides; returns false on timeout.
+__device__ __forceinline__ bool mbar_wait_ns(uint32_t mbar, uint32_t parity, uint64_t limit_ns) {
+  const uint64_t t0 = global_ns();
+  for (uint32_t it = 0; it < (1u << 30); it++) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
@@ -66,9 +75,14 @@ __device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity) {
         : "=r"(done)
         : "r"(mbar), "r"(parity));
     if (done) return true;
+    if (global_ns() - t0 > limit_ns) return false;
   }
   return false;
 }
+
+// the kernels' waits (tensor-core results, TMA tiles) give up after one second
+constexpr uint64_t kWaitLimitNs = 1000000000ull;
+__device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity) { return mbar_wait_ns(mbar, parity, kWaitLimitNs); }
 
 #define AFFT_TMEM_LD8(taddr, r)                                                                          \
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"                  \

@@ -253,6 +253,12 @@ AFFT_GB300_API int afft_gb300_tuned(int kind, size_t ndim, const size_t* dim, si
  * polls, and returns AFFT_GB300_ETIMEOUT when the kernel gave up and
  * reported it as designed (-1 on a CUDA error).  Nothing faults or hangs. */
 AFFT_GB300_API int afft_gb300_selftest_bounded_wait(int iters);
+/* Self-test of the cols passes' TMA tile wait (no counterpart in afft): a
+ * kernel issues one tensor-map copy into shared memory while announcing
+ * twice its bytes, so the wait never completes; the kernels' time-bounded
+ * wait gives up after `limit_us` microseconds and the call returns
+ * AFFT_GB300_ETIMEOUT (-1 on a CUDA error).  Nothing faults or hangs. */
+AFFT_GB300_API int afft_gb300_selftest_tma_wait(int limit_us);
 
 /* Number of this library's kernel launches one transform of `plan` issues. */
 AFFT_GB300_API int afft_gb300_plan_launches(const void* plan);

@@ -83,6 +83,22 @@ def test_bounded_wait_reports_timeout(dev):
     assert yr[0] == 256.0 and yi[0] == 256.0
 
 
+def test_tma_tile_wait_reports_timeout(dev):
+    # the cols passes' TMA tile wait, made to run out on purpose (a copy of
+    # half the announced bytes): 20 ms limit, reported as ETIMEOUT
+    f = G.lib().afft_gb300_selftest_tma_wait
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_int]
+    assert f(20000) == 6, G.last_error()
+    # the context is still usable: a TMA-fed cols pass runs and is right
+    p = G.BatchPlan("c", [256, 256], 4)
+    x = torch.ones(256 * 256 * 4, device=dev)
+    yr, yi = torch.zeros_like(x), torch.zeros_like(x)
+    p(x, x, yr, yi)
+    torch.cuda.synchronize()
+    assert float(yr[0]) == 65536.0 and float(yr[1:65536].abs().max()) == 0.0
+
+
 def test_missing_data_pointers_are_rejected(dev):
     # a NULL array the transform reads or writes is reported (EINVAL) before
     # anything is launched, through the synchronous, async and queue entry
