@@ -142,8 +142,15 @@ const float2* stage_twiddles(int logl);
 const float2* real_twiddles(long long L);         // W_{2L}^k, k < L
 void fourstep_tables(long long N, const float2** hi, const float2** lo, int* lo_bits);
 // The four-step twiddle as one matrix, W_N^{t2 k} at [t2 * L1 + k], for
-// N <= kFullTableMax (nullptr above): one coalesced load per element.
-constexpr long long kFullTableMax = 1LL << 20;
+// N <= kFullTableMax (nullptr above): one coalesced load per element.  It
+// covers every four-step axis a plan builds (up to 2^22 points: 32 MB), so
+// each plan's four-step twiddle is computed in FP64 and rounded once; the
+// hi/lo product form remains for the no-allocation entry point's fixed
+// arrays.
+#ifndef AFFT_FULL_TABLE_LOG
+#define AFFT_FULL_TABLE_LOG 22
+#endif
+constexpr long long kFullTableMax = 1LL << AFFT_FULL_TABLE_LOG;
 const float2* fourstep_full_table(long long N, long long L2);
 // FP64 tables (computed in FP64, no rounding): stage twiddles of the FP64
 // line kernels, W_{2L}^k (k < L), and the four-step matrix W_N^{t2 k} at
