@@ -51,3 +51,30 @@ def test_reference_cxx_wrapper_round_trips_on_the_gpu(tmp_path):
     assert r.returncode == 0, r.stdout + r.stderr
     # both precisions ran their transforms (not the empty-plan path)
     assert r.stdout.count("round trip rel-L2") == 2, r.stdout
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(_wrapper_dir() is None or not os.path.exists(os.path.join(_wrapper_dir(), "doit.cpp"))
+                    and not os.path.exists(os.path.join(_wrapper_dir(), "misc", "libbench2-test", "doit.cpp")),
+                    reason="afft's libbench2 test program is absent (no reference or staged sources)")
+def test_libbench2_program_runs_on_the_gpu(tmp_path):
+    """afft's libbench2 test program (misc/libbench2-test/doit.cpp), unchanged,
+    driven the way the libbench2 harness drives it (tests/cxx/bench2_main.cpp
+    with a restatement of the harness's user interface), through fft.hpp on
+    interleaved data: forward and backward 1D-3D problems against a naive
+    DFT."""
+    if not cuda_available():
+        pytest.skip("no CUDA device")
+    src = _wrapper_dir()
+    doit = os.path.join(src, "doit.cpp")
+    if not os.path.exists(doit):
+        doit = os.path.join(src, "misc", "libbench2-test", "doit.cpp")
+    exe = str(tmp_path / "bench2")
+    libdir = os.path.dirname(G.LIB_PATH)
+    cmd = ["g++", "-std=c++17", "-O1", "-I", os.path.join(HERE, "libbench2"), "-I", HERE, "-I", src, doit,
+           os.path.join(HERE, "bench2_main.cpp"), "-L", libdir, "-lafft_gb300", "-Wl,-rpath," + libdir, "-o", exe]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.strip().endswith("ok") and r.stdout.count("rel-L2") == 10, r.stdout
