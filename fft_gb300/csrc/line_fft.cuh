@@ -28,6 +28,11 @@
 // time and fall back to 4-byte accesses (callers may pass any 4-byte-aligned
 // array).
 //
+// Cols passes of 256 to 1024 points (and the 2048-point C2R pass) also come
+// in a TMA-fed form (line_fft_tma): one thread loads the CTA's input tile
+// into the exchange buffer with tensor-map copies on an mbarrier, and the
+// threads read their canonical elements from shared memory.
+//
 // This restates the work of afft's onedim.hpp (radix-4/8/16 passes,
 // onedim.hpp:55-507) and multi.hpp (passes along strided dims,
 // multi.hpp:18-259) as one self-sorting (Stockham) formulation, so no
