@@ -6,7 +6,9 @@
 //    on dst.  An axis of length <= 2^14 (contiguous) or <= 2^11 (strided) is
 //    one pass; a longer axis takes two passes (four-step: L = L1*L2, a pass
 //    over L1 with the W_L^{t2 k1} twiddle fused into its epilogue, then a pass
-//    over L2), through a plan-owned scratch buffer.
+//    over L2), through a plan-owned scratch buffer.  Contiguous complex axes
+//    of 2^21 and 2^22 points take three: L1 = 256, then the L2 pass as a
+//    strided four-step of its own.
 //  - inverse (fft_internal.hpp:166-198): the same passes with re/im swapped
 //    on load and store.
 //  - real 1D (onedim.hpp:1110-1254): the n/2-point complex transform of the
@@ -365,6 +367,10 @@ static View inter_view(int b, long long off = 0) {  // re,im pairs in one array
 #ifndef AFFT_TMA_C2C11
 #define AFFT_TMA_C2C11 0
 #endif
+// 1D complex axes from 2^AFFT_THREE_PASS_LOG points run as three passes
+#ifndef AFFT_THREE_PASS_LOG
+#define AFFT_THREE_PASS_LOG 21
+#endif
 // ... and of the transposing-store passes (four-step pass A)
 #ifndef AFFT_TMA_TSTORE
 #define AFFT_TMA_TSTORE 1
@@ -610,9 +616,14 @@ struct Builder {
         line(LK_C2C, false, false, logl, io(A, 1, 0, a_bs, 0, 0), io(B, 1, 0, b_bs, 0, 0), outer, inverse);
         return;
       }
-      // four-step along a contiguous axis
-      int l1 = l1_of(logl), l2 = logl - l1;
-      if (l1 > COLS_MAX_LOG || l2 > COLS_MAX_LOG) {
+      // four-step along a contiguous axis; from 2^AFFT_THREE_PASS_LOG points
+      // (FP32) pass A takes 256 points and pass B becomes a strided
+      // four-step of its own: three passes of 64 to 256 points instead of two
+      // of 1024 / 2048, whose one-CTA-per-SM tiles run at about half the
+      // rate per pass
+      const bool three = !f64 && logl >= AFFT_THREE_PASS_LOG && !tune.two_pass;
+      int l1 = three ? 8 : l1_of(logl), l2 = logl - l1;
+      if (l1 > COLS_MAX_LOG || (l2 > COLS_MAX_LOG && !three)) {
         fail("axis longer than 2^22 points");
         return;
       }
@@ -624,6 +635,15 @@ struct Builder {
       line(LK_C2C, true, true, l1, io(A, L2, 1, a_bs, l2, L2 - 1), io(S, 1, L1, L, l2, L2 - 1),
            outer * L2, inverse, L, L2 - 1, 0);
       // pass B: lines (o, k1), points t2 -> X[o][k1 + L1 k2]
+      if (l2 > COLS_MAX_LOG) {
+        // the same as a strided axis: (outer, L2, inner L1) from Y to X,
+        // its own scratch above Y's
+        const long long save = scr_base;
+        scr_base += 2 * outer * L;
+        axis(outer, L2, L1, S, B, inverse, L, b_bs);
+        scr_base = save;
+        return;
+      }
       line(LK_C2C, true, false, l2, io(S, L1, 1, L, l1, L1 - 1), io(B, L1, 1, b_bs, l1, L1 - 1),
            outer * L1, inverse);
       return;
