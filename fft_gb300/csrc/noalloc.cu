@@ -144,7 +144,7 @@ extern "C" int afft_gb300_c2c_noalloc(const float* src_re, const float* src_im, 
   // the launch list of the ordinary plan in its two-pass form (the one the
   // fixed scratch array is sized for), built without touching the device
   Tuning two;
-  two.two_pass = 1;
+  two.passes = 2;
   auto P = build_plan(inverse ? K_CI : K_C, 1, dims, (long long)batch, afft_split, true, 0, &two);
   if (!P || P->scratch_elems > 2 * kNoallocMaxElems) {
     set_error(AFFT_GB300_EINVAL, "no-alloc transform: unsupported shape");

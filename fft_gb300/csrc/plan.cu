@@ -621,7 +621,8 @@ struct Builder {
       // four-step of its own: three passes of 64 to 256 points instead of two
       // of 1024 / 2048, whose one-CTA-per-SM tiles run at about half the
       // rate per pass
-      const bool three = !f64 && logl >= AFFT_THREE_PASS_LOG && !tune.two_pass;
+      const bool three =
+          !f64 && (tune.passes == 3 ? logl >= 20 : tune.passes == 2 ? false : logl >= AFFT_THREE_PASS_LOG);
       int l1 = three ? 8 : l1_of(logl), l2 = logl - l1;
       if (l1 > COLS_MAX_LOG || (l2 > COLS_MAX_LOG && !three)) {
         fail("axis longer than 2^22 points");

@@ -105,7 +105,8 @@ struct Tuning {
   int cols_lsu = 0;   // 1: cols passes load their tiles through the LSU even where TMA applies
   int tc = 0;         // 1: the split-precision tensor-core form where a pass has one
   int cols_c = 0;     // lines per CTA of the 256- and 512-point complex cols passes (0: the default)
-  int two_pass = 0;   // 1: 1D complex axes of 2^21 and 2^22 points in two passes, not three
+  int passes = 0;     // 1D complex axes of 2^20 points and more: 0 the built-in rule (three passes
+                      // from 2^21), 2 two passes, 3 three passes
 };
 // The tuned choice for a shape on the current device, if the autotuner has
 // one (tuning it first when AFFT_GB300_AUTOTUNE=1); else the defaults.

@@ -11,7 +11,7 @@
 //  - the tile width (lines per CTA) of 256- and 512-point complex cols passes;
 //  - the plain FP32 form or the split-precision tensor-core form of the
 //    passes that have one;
-//  - 1D complex axes of 2^21 and 2^22 points in three passes or two.
+//  - 1D complex axes of 2^20 to 2^22 points in two passes or three.
 // Each distinct variant (distinct kernels or launch shapes) is built as a
 // device plan and timed with CUDA events on zeroed buffers of the current
 // device (2 warm-up and 5 timed launches, median).  Choices live in a
@@ -79,8 +79,8 @@ std::string key_of(int kind, int ndim, const long long* dims, long long batch, i
 }
 
 // file format: a JSON object, one entry per line:
-//   "<key>": {"split": S, "real_inv": R, "cols_lsu": U, "tc": T, "cols_c": C, "two_pass": P, "ms": M},
-// (entries of the older forms, without two_pass or cols_lsu / tc / cols_c,
+//   "<key>": {"split": S, "real_inv": R, "cols_lsu": U, "tc": T, "cols_c": C, "passes": P, "ms": M},
+// (entries of the older forms, without passes or cols_lsu / tc / cols_c,
 // still load)
 void load_locked(TuneCache& C) {
   if (C.loaded) return;
@@ -99,8 +99,8 @@ void load_locked(TuneCache& C) {
     Entry e;
     if (std::sscanf(b + 1,
                     " : {\"split\": %d, \"real_inv\": %d, \"cols_lsu\": %d, \"tc\": %d, \"cols_c\": %d, "
-                    "\"two_pass\": %d, \"ms\": %lf",
-                    &e.t.split, &e.t.real_inv, &e.t.cols_lsu, &e.t.tc, &e.t.cols_c, &e.t.two_pass, &e.ms) == 7 ||
+                    "\"passes\": %d, \"ms\": %lf",
+                    &e.t.split, &e.t.real_inv, &e.t.cols_lsu, &e.t.tc, &e.t.cols_c, &e.t.passes, &e.ms) == 7 ||
         std::sscanf(b + 1,
                     " : {\"split\": %d, \"real_inv\": %d, \"cols_lsu\": %d, \"tc\": %d, \"cols_c\": %d, \"ms\": %lf",
                     &e.t.split, &e.t.real_inv, &e.t.cols_lsu, &e.t.tc, &e.t.cols_c, &e.ms) == 6 ||
@@ -122,8 +122,8 @@ void save_locked(const TuneCache& C) {
     const Tuning& t = kv.second.t;
     std::fprintf(f,
                  "\"%s\": {\"split\": %d, \"real_inv\": %d, \"cols_lsu\": %d, \"tc\": %d, \"cols_c\": %d, "
-                 "\"two_pass\": %d, \"ms\": %.6f}%s\n",
-                 kv.first.c_str(), t.split, t.real_inv, t.cols_lsu, t.tc, t.cols_c, t.two_pass, kv.second.ms,
+                 "\"passes\": %d, \"ms\": %.6f}%s\n",
+                 kv.first.c_str(), t.split, t.real_inv, t.cols_lsu, t.tc, t.cols_c, t.passes, kv.second.ms,
                  ++i < C.table.size() ? "," : "");
   }
   std::fprintf(f, "}\n");
@@ -187,11 +187,12 @@ int tune_shape(int kind, int ndim, const long long* dims, long long batch, int f
   std::vector<std::pair<Tuning, std::unique_ptr<Plan>>> cands;
   std::vector<std::string> sigs;
   static const int widths[] = {0, 8, 16, 32};
-  // the two-pass form of long 1D axes only where a dimension has one
+  // two or three passes for long 1D axes, only where a dimension has one
   long long maxdim = 1;
   for (int i = 0; i < ndim; i++) maxdim = std::max(maxdim, dims[i]);
-  const int npass = maxdim >= (1LL << 21) ? 2 : 1;
-  for (int two = 0; two < npass; two++)
+  static const int pass_forms[] = {0, 2, 3};
+  const int npass = maxdim >= (1LL << 20) ? 3 : 1;
+  for (int pf = 0; pf < npass; pf++)
   for (int split = 0; split < 2; split++)
     for (int real_inv = 0; real_inv < 2; real_inv++)
       for (int lsu = 0; lsu < 2; lsu++)
@@ -203,7 +204,7 @@ int tune_shape(int kind, int ndim, const long long* dims, long long batch, int f
             t.cols_lsu = lsu;
             t.tc = tc;
             t.cols_c = w;
-            t.two_pass = two;
+            t.passes = pass_forms[pf];
             auto P = build_plan(kind, ndim, dims, batch, format, false, 0, &t);
             if (!P) {
               clear_error();
@@ -254,17 +255,17 @@ int tune_shape(int kind, int ndim, const long long* dims, long long batch, int f
     for (size_t i = 0; i < cands.size(); i++) {
       const Tuning& t = cands[i].first;
       snprintf(buf, sizeof buf,
-               "%s{\"split\":%d,\"real_inv\":%d,\"cols_lsu\":%d,\"tc\":%d,\"cols_c\":%d,\"two_pass\":%d,"
+               "%s{\"split\":%d,\"real_inv\":%d,\"cols_lsu\":%d,\"tc\":%d,\"cols_c\":%d,\"passes\":%d,"
                "\"launches\":%zu,\"ms\":%.6f}",
-               i ? "," : "", t.split, t.real_inv, t.cols_lsu, t.tc, t.cols_c, t.two_pass, cands[i].second->ops.size(),
+               i ? "," : "", t.split, t.real_inv, t.cols_lsu, t.tc, t.cols_c, t.passes, cands[i].second->ops.size(),
                times[i]);
       *report += buf;
     }
     const Tuning& t = out->t;
     snprintf(buf, sizeof buf,
-             "],\"chosen\":{\"split\":%d,\"real_inv\":%d,\"cols_lsu\":%d,\"tc\":%d,\"cols_c\":%d,\"two_pass\":%d,"
+             "],\"chosen\":{\"split\":%d,\"real_inv\":%d,\"cols_lsu\":%d,\"tc\":%d,\"cols_c\":%d,\"passes\":%d,"
              "\"ms\":%.6f}}",
-             t.split, t.real_inv, t.cols_lsu, t.tc, t.cols_c, t.two_pass, out->ms);
+             t.split, t.real_inv, t.cols_lsu, t.tc, t.cols_c, t.passes, out->ms);
     *report += buf;
   }
   return 0;

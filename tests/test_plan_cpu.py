@@ -65,7 +65,11 @@ def test_launch_counts():
     assert len(describe("r", [1 << 20], 2)["ops"]) == 2
     assert len(describe("ri", [1 << 19], 2)["ops"]) == 2
     assert len(describe("ri", [1 << 20], 2)["ops"]) == 3   # standalone pre-pass measured faster there
-    assert len(describe("ri", [1 << 22], 1)["ops"]) == 3
+    # (the standalone pre-pass, then the complex 2^21 axis in three passes)
+    assert len(describe("ri", [1 << 22], 1)["ops"]) == 4
+    # complex axes of 2^21 and 2^22 points: three passes
+    assert len(describe("c", [1 << 22], 1)["ops"]) == 3
+    assert len(describe("ci", [1 << 21], 2)["ops"]) == 3
 
 
 # FP64 plans (afft_64_*): rows up to 2^13 points, cols up to 2^11, standalone
