@@ -54,6 +54,18 @@ def test_plan_emulation(kind, dims):
             assert O.rel_l2(got, ref) < 1e-12, (kind, dims, batch, fmt)
 
 
+@pytest.mark.parametrize("kind,fmt", [("c", G.afft_split), ("ci", G.afft_interleaved), ("ri", G.afft_split)])
+def test_plan_emulation_three_pass_2p22(kind, fmt):
+    # the 2^22-point complex axis in three passes (256, then a strided
+    # four-step through a second scratch region); one format per kind keeps
+    # the CPU time to seconds
+    dims = [1 << 22]
+    desc = describe(kind, dims, 1, fmt)
+    a, b = _inputs(kind, dims, 1, 22)
+    got = run(desc, a, b)
+    assert O.rel_l2(got, _expected(kind, dims, 1, a, b)) < 1e-12
+
+
 def test_launch_counts():
     # one pass while a line fits one CTA, two (four-step) beyond
     assert len(describe("c", [4096], 16384)["ops"]) == 1
