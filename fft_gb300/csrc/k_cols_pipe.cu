@@ -1,0 +1,13 @@
+// 2048-point cols passes in the persistent TMA-pipelined form (line_fft_pipe)
+#include "kernels.h"
+namespace agb {
+bool get_cols_pipe(int logl, int kind, LineKernel* out) {
+  if (logl != 11) return false;
+  switch (kind) {
+    case LK_C2C: *out = make_pipe_kernel<11, LK_C2C>(); return true;
+    case LK_R2C: *out = make_pipe_kernel<11, LK_R2C>(); return true;
+    case LK_C2R: *out = make_pipe_kernel<11, LK_C2R>(); return true;
+  }
+  return false;
+}
+}  // namespace agb

@@ -2,12 +2,14 @@
 // family so they compile in parallel).
 #pragma once
 #include "line_fft.cuh"
+#include "line_fft_pipe.cuh"
 
 namespace agb {
 
 typedef void (*LineKernelFn)(LineParams);
 typedef void (*GroupedKernelFn)(const Segment*, const int*, long long);
 typedef void (*LineKernelTmaFn)(LineParams, TmaTile);
+typedef void (*LineKernelPipeFn)(LineParams, TmaTile, long long);
 
 struct LineKernel {
   LineKernelFn fn;
@@ -27,6 +29,9 @@ struct LineKernel {
   LineKernelTmaFn tma; // the same pass with its input tile loaded by TMA (cols passes over
                        // split planes), or null
   GroupedKernelFn grouped_tma;   // its grouped form (queue segments with tensor maps), or null
+  LineKernelPipeFn pipe = nullptr;   // the persistent TMA-pipelined form (line_fft_pipe), or null;
+                                     // launched on at most one CTA per SM with the tile count
+  size_t pipe_smem = 0;              // its dynamic shared memory (raw tile + exchange buffer)
 };
 
 constexpr int ROWS_MAX_LOG = 14;   // rows mode: one CTA up to 16384 points
@@ -73,6 +78,11 @@ bool get_cols_tma_tstore(int logl, LineKernel* out);
 // 3), plain or with the transposing store, 2^8 and 2^9 points, with TMA
 // loads of the interleaved tile (k_cols_tma_pairs.cu)
 bool get_cols_tma_pairs(int logl, bool tstore, int pairs, LineKernel* out);
+
+// 2048-point cols passes {C2C, R2C (unsplit), C2R} over split planes in the
+// persistent TMA-pipelined form (k_cols_pipe.cu): out->pipe set, out->tma and
+// out->fn the one-tile-per-CTA kernels of the same shape
+bool get_cols_pipe(int logl, int kind, LineKernel* out);
 
 // cols c2c passes (not transposing) with another tile width, for the
 // autotuner: 256 points in 8 or 32 lines, 512 points in 16; TMA-fed
@@ -158,6 +168,17 @@ LineKernel make_tma_kernel() {
   LineKernel k = make_line_kernel<LOGL, true, KIND, TSTORE, false, UNIT, C>();
   k.tma = &line_fft_tma<LOGL, C, KIND, TSTORE, UNIT>;
   k.grouped_tma = &line_fft_grouped<LOGL, C, true, KIND, TSTORE, false, UNIT, true>;
+  return k;
+}
+
+// a 2048-point cols pass with its pipelined form (8 lines per tile)
+template <int LOGL, int KIND>
+LineKernel make_pipe_kernel() {
+  constexpr int C = 8;
+  LineKernel k = make_tma_kernel<LOGL, KIND, C>();
+  k.pipe = &line_fft_pipe<LOGL, C, KIND>;
+  static_assert(LOGL == 11, "the pipelined kernels are built for 2048-point lines");
+  k.pipe_smem = ((size_t)2 * (1 << LOGL) + kPipeRows) * C * sizeof(float);   // raw tile + exchange rows
   return k;
 }
 

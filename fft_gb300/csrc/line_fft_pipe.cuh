@@ -1,0 +1,259 @@
+// Persistent, TMA-pipelined cols passes of 2048 points (line_fft_pipe).
+//
+// A 2048-point cols tile of 8 lines is 128 KB, so the one-tile-per-CTA
+// kernels (line_fft, line_fft_tma) fit one CTA per SM.  Each SM then loads
+// a tile, runs its stages and stores it in sequence, and HBM idles while the
+// SMs compute.  Here one CTA per SM walks the tiles blockIdx.x,
+// blockIdx.x + gridDim.x, ...  As soon as its threads have taken tile i out
+// of the raw buffer (into registers), one thread issues the TMA loads of the
+// CTA's next tile into that buffer.  Those land while tile i's stages run and
+// its results are stored.
+//
+// Shared memory: the raw tile ([re: L rows x C][im: L rows x C] floats,
+// 128 KB, as tma_load_tile lays it out) and a separate exchange buffer through
+// which the stages pass the re parts first, then the im parts.  Element j of
+// line c sits at float (j + j/8) * C + c there (one pad row per 8: 72 KB).  A
+// warp covers 4 consecutive threads t (lanes 8 apart share a line), so each
+// access touches 4 rows, and the padding puts them on 4 different 8-bank
+// groups for the radix-8 scatter (rows 8 apart), the radix-16 scatter
+// (consecutive rows) and the canonical gather: one wavefront per access.  Each
+// pattern's row is a per-thread base plus a compile-time offset per element.
+//
+// Every wait on the tile barrier is bounded (one second); a timeout sets the
+// error word to 2, waits once more (bounded) for the copies in flight, and the
+// CTA returns.
+#pragma once
+#include "line_fft.cuh"
+
+namespace agb {
+
+// Rows of the exchange buffer for the 2048-point schedule (radix 8, 16, 16;
+// T = 128, E = 16).  Stage 0 scatters output e = u + 2 r of butterfly
+// b = t + 128 u to element 8 b + r, stage 1 output e of butterfly t to element
+// 128 (t / 8) + t % 8 + 8 e, and the gather takes element t + 128 e; with
+// row = j + j/8 these are base(t) + offset(e).
+constexpr int kPipeRows = 2048 + 2048 / 8;
+template <int S>
+__device__ __forceinline__ int pipe_wbase(int t) {
+  return S == 0 ? 9 * t : 144 * (t >> 3) + (t & 7);
+}
+template <int S>
+__host__ __device__ constexpr int pipe_woff(int e) {
+  return S == 0 ? 1152 * (e % 2) + e / 2 : 9 * e;
+}
+__device__ __forceinline__ int pipe_gbase(int t) { return t + (t >> 3); }
+__host__ __device__ constexpr int pipe_goff(int e) { return 144 * e; }
+__device__ __forceinline__ int pipe_row(int j) { return j + (j >> 3); }
+
+// The exchange after stage S: every value to its stage-S position, then
+// element t + T e of this thread's line back, re parts first, then im parts.
+// TRAIL: the buffer is written again before the next CTA-wide barrier.
+template <int LOGL, int C, int S, bool TRAIL>
+__device__ __forceinline__ void pipe_exchange(float2 (&v)[Sched<LOGL>::E], int t, int c, float* xs) {
+  constexpr int E = Sched<LOGL>::E;
+  float* w = xs + pipe_wbase<S>(t) * C + c;
+  const float* g = xs + pipe_gbase(t) * C + c;
+  float nx[E];
+#pragma unroll
+  for (int e = 0; e < E; e++) w[pipe_woff<S>(e) * C] = v[e].x;
+  __syncthreads();
+#pragma unroll
+  for (int e = 0; e < E; e++) nx[e] = g[pipe_goff(e) * C];
+  __syncthreads();
+#pragma unroll
+  for (int e = 0; e < E; e++) w[pipe_woff<S>(e) * C] = v[e].y;
+  __syncthreads();
+#pragma unroll
+  for (int e = 0; e < E; e++) v[e] = make_float2(nx[e], g[pipe_goff(e) * C]);
+  if constexpr (TRAIL) __syncthreads();
+}
+
+// All stages of one tile, values in registers in the canonical layout on
+// entry and exit (as run_stages).
+template <int LOGL, int C, int KIND, int S>
+__device__ __forceinline__ void pipe_stages(float2 (&v)[Sched<LOGL>::E], int t, int c, const float2* tw,
+                                            float* xs) {
+  using Sc = Sched<LOGL>;
+  if constexpr (S < Sc::NSTAGES) {
+    constexpr int R = Sc::radix(S), NS = Sc::ns(S);
+    // the butterflies with their outputs kept in registers (stage()'s last-stage form)
+    stage<R, NS, Sc::E, Sc::T, true, false, 0, packed_bfly<LOGL, true>()>(v, t, c, tw + Sc::twoff(S), xs, false,
+                                                                         nullptr);
+    if constexpr (S + 1 < Sc::NSTAGES) {
+      pipe_exchange<LOGL, C, S, (S + 2 < Sc::NSTAGES || KIND == LK_R2C)>(v, t, c, xs);
+      pipe_stages<LOGL, C, KIND, S + 1>(v, t, c, tw, xs);
+    }
+  }
+}
+
+// Issue the TMA loads of tile `tile` (C adjacent columns of one outer block,
+// both planes, boxes of C columns x box_rows rows) on the barrier at mb.
+template <int L, int C>
+__device__ __forceinline__ void pipe_issue(const LineParams& p, const TmaTile& tm, long long tile, uint32_t raw,
+                                           uint32_t mb) {
+  const long long q0 = tile * C;
+  const int col = (int)(q0 & p.in.qmask);
+  const int outer = (int)(q0 >> p.in.qshift);
+  constexpr uint32_t plane = (uint32_t)L * C * 4u;
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(2u * plane) : "memory");
+  for (int r = 0; r < L; r += tm.box_rows) {
+    tma_load_3d(raw + (uint32_t)r * C * 4u, &tm.re, col, r, outer, mb);
+    tma_load_3d(raw + plane + (uint32_t)r * C * 4u, &tm.im, col, r, outer, mb);
+  }
+}
+
+// KIND: LK_C2C (with the four-step twiddle when p.tw_n), LK_R2C (unsplit:
+// the post-pass through the exchange buffer), LK_C2R (the pre-pass from the
+// raw tile, bin L read directly).  Split planes in, split planes out; every
+// tile whole (the host's tma_tile rules).  ntiles = nlines / C.
+template <int LOGL, int C, int KIND>
+__global__ void __launch_bounds__(Sched<LOGL>::T * C, 1)
+line_fft_pipe(const LineParams p, const __grid_constant__ TmaTile tm, long long ntiles) {
+  using Sc = Sched<LOGL>;
+  constexpr int L = Sc::L, E = Sc::E, T = Sc::T;
+  static_assert(KIND == LK_C2C || KIND == LK_R2C || KIND == LK_C2R, "plain cols kinds");
+  static_assert(LOGL == 11 && C == 8 && T == 128 && E == 16 && Sc::radix(0) == 8,
+                "the exchange rows are those of 8-line 2048-point tiles");
+  __shared__ __align__(8) uint64_t mbar;
+  extern __shared__ __align__(1024) float2 smem_raw[];
+  float* raw = reinterpret_cast<float*>(smem_raw);
+  float* xs = raw + 2 * L * C;
+  const int tid = threadIdx.x;
+  const int c = tid % C, t = tid / C;
+  const uint32_t mb = smem_u32(&mbar);
+  const uint32_t raw_s = smem_u32(raw);
+
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncthreads();
+  if (tid == 0 && (long long)blockIdx.x < ntiles) pipe_issue<L, C>(p, tm, blockIdx.x, raw_s, mb);
+
+  uint32_t phase = 0;
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, phase ^= 1u) {
+    if (!__syncthreads_and(tc_wait(mb, phase))) {
+      if (tid == 0) {
+        if (p.err) atomicExch(p.err, 2);
+        tc_wait(mb, phase);   // let copies still in flight land before shared memory goes away
+      }
+      __syncthreads();
+      return;
+    }
+    const long long q = tile * C + c;
+    float2 v[E];
+    if constexpr (KIND == LK_C2R) {
+      // real inverse pre-pass (onedim.hpp:1064-1068 / multi.hpp:366-370 with
+      // inverse): Z'[i] = a - i b, a = X[i] + conj(X[L-i]),
+      // b = (conj(X[L-i]) - X[i]) conj(w_i); Z'[0] from the real parts of
+      // X[0] and X[L]; then the inverse transform of Z' (swap trick)
+      float2 bl = make_float2(0.f, 0.f);
+      if (t == 0) {
+        const long long oL = line_off(p.in, q) + (long long)L * p.in.es;
+        bl = make_float2(__ldg(p.in.re + oL), __ldg(p.in.im + oL));
+      }
+#pragma unroll
+      for (int e = 0; e < E; e++) {
+        const int i = t + T * e;
+        const float2 s0 = make_float2(raw[i * C + c], raw[L * C + i * C + c]);
+        const int im = (L - i) & (L - 1);
+        const float2 s1 = i == 0 ? bl : make_float2(raw[im * C + c], raw[L * C + im * C + c]);
+        float2 z;
+        if (i == 0) {
+          z = make_float2(s0.x + s1.x, s0.x - s1.x);
+        } else {
+          const float2 w = ldg2(p.rtw + i);
+          const float2 a = cadd(s0, cconj(s1));
+          const float2 b = cmul(csub(cconj(s1), s0), cconj(w));
+          z = cadd(a, cmul_negi(b));
+        }
+        v[e] = cswap(z);
+      }
+    } else {
+#pragma unroll
+      for (int e = 0; e < E; e++) {
+        const int i = t + T * e;
+        v[e] = make_float2(raw[i * C + c], raw[L * C + i * C + c]);
+      }
+      if (KIND == LK_C2C && p.inverse) {
+#pragma unroll
+        for (int e = 0; e < E; e++) v[e] = cswap(v[e]);
+      }
+    }
+    // every thread has its tile: the raw buffer takes the next one
+    __syncthreads();
+    if (tid == 0 && tile + gridDim.x < ntiles) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      pipe_issue<L, C>(p, tm, tile + gridDim.x, raw_s, mb);
+    }
+
+    pipe_stages<LOGL, C, KIND, 0>(v, t, c, p.tw, xs);
+
+    const long long base = line_off(p.out, q);
+    const long long S = (long long)T * p.out.es;
+    float* pr = p.out.re + base + (long long)t * p.out.es;
+    float* pi = p.out.im + base + (long long)t * p.out.es;
+    if constexpr (KIND == LK_C2C) {
+      if (p.tw_n && p.tw_full) {
+#pragma unroll
+        for (int e = 0; e < E; e++) v[e] = cmul(v[e], fourstep_twiddle<L, true>(p, q, t + T * e));
+      } else if (p.tw_n) {
+#pragma unroll
+        for (int e = 0; e < E; e++) v[e] = cmul(v[e], fourstep_twiddle<L, false>(p, q, t + T * e));
+      }
+      if (p.inverse) {
+#pragma unroll
+        for (int e = 0; e < E; e++) v[e] = cswap(v[e]);
+      }
+#pragma unroll
+      for (int e = 0; e < E; e++) {
+        pr[e * S] = v[e].x;
+        pi[e * S] = v[e].y;
+      }
+    } else if constexpr (KIND == LK_C2R) {
+#pragma unroll
+      for (int e = 0; e < E; e++) {
+        pr[e * S] = v[e].y;   // swapped back: re of the output is im of the swapped transform
+        pi[e * S] = v[e].x;
+      }
+    } else {
+      // real forward post-pass (onedim.hpp:1058-1108 / multi.hpp:354-414):
+      // X[k] = a - i b, a = (Z[k] + conj(Z[L-k]))/2,
+      // b = (Z[k] - conj(Z[L-k])) w_k / 2; X[0], X[L] from Z[0].  The mirror
+      // Z[L-k] comes through the exchange buffer, re parts then im parts.
+      float mx[E];
+#pragma unroll
+      for (int e = 0; e < E; e++) xs[(pipe_gbase(t) + pipe_goff(e)) * C + c] = v[e].x;
+      __syncthreads();
+#pragma unroll
+      for (int e = 0; e < E; e++) mx[e] = xs[pipe_row((L - (t + T * e)) & (L - 1)) * C + c];
+      __syncthreads();
+#pragma unroll
+      for (int e = 0; e < E; e++) xs[(pipe_gbase(t) + pipe_goff(e)) * C + c] = v[e].y;
+      __syncthreads();
+#pragma unroll
+      for (int e = 0; e < E; e++) {
+        const int k = t + T * e;
+        const float2 s0 = v[e];
+        const float2 s1 = make_float2(mx[e], xs[pipe_row((L - k) & (L - 1)) * C + c]);
+        float2 x;
+        if (k == 0) {
+          x = make_float2(s0.x + s0.y, 0.f);
+          const long long aL = base + (long long)L * p.out.es;
+          p.out.re[aL] = s0.x - s0.y;
+          p.out.im[aL] = 0.f;
+        } else {
+          const float2 w = ldg2(p.rtw + k);
+          const float2 a = make_float2(0.5f * (s0.x + s1.x), 0.5f * (s0.y - s1.y));
+          const float2 d = make_float2(0.5f * (s0.x - s1.x), 0.5f * (s0.y + s1.y));
+          x = cadd(a, cmul_negi(cmul(d, w)));
+        }
+        pr[e * S] = x.x;
+        pi[e * S] = x.y;
+      }
+    }
+  }
+}
+
+}  // namespace agb

@@ -385,6 +385,16 @@ static View inter_view(int b, long long off = 0) {  // re,im pairs in one array
 #ifndef AFFT_TMA_C2R11
 #define AFFT_TMA_C2R11 1
 #endif
+// 2048-point cols passes over split planes: the persistent TMA-pipelined
+// kernels (one CTA per SM loading its next tile under the current one's stages)
+#ifndef AFFT_COLS_PIPE
+#define AFFT_COLS_PIPE 1
+#endif
+// the 2048-point R2C pass in that form too (unsplit), instead of the split
+// one-tile-per-two-CTAs form
+#ifndef AFFT_PIPE_R2C
+#define AFFT_PIPE_R2C 0
+#endif
 
 static IOSpec io(const View& v, long long es, long long lo, long long hi, int qshift, long long qmask) {
   IOSpec s;
@@ -487,6 +497,14 @@ struct Builder {
           kt.tstore == op.k.tstore && !op.k.tc)
         op.k = kt;
     }
+    // 2048-point cols passes: the persistent pipelined form (the R2C pass
+    // unsplit); at launch the one-tile-per-CTA kernels of the same shape run
+    // where the bound arrays miss the TMA rules
+    LineKernel kp;
+    if (AFFT_COLS_PIPE && !f64 && !tc && cols && !tstore && cpairs == 0 && !tune.cols_lsu && !tune.no_pipe &&
+        (kind == LK_C2C || (kind == LK_R2C && AFFT_PIPE_R2C) || kind == LK_C2R) && get_cols_pipe(logl, kind, &kp) &&
+        kp.kind == op.k.kind && kp.logl == op.k.logl && !op.k.tc)
+      op.k = kp;
     // another tile width for 256- and 512-point complex cols passes, when tuned so
     LineKernel ka;
     if (tune.cols_c && !f64 && !tc && cols && !tstore && !cpairs && kind == LK_C2C &&
@@ -507,7 +525,9 @@ struct Builder {
           (cudaFuncSetAttribute((const void*)op.k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)op.k.smem) != cudaSuccess ||
            (op.k.tma && cudaFuncSetAttribute((const void*)op.k.tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)op.k.smem) != cudaSuccess))) {
+                                             (int)op.k.smem) != cudaSuccess) ||
+           (op.k.pipe && cudaFuncSetAttribute((const void*)op.k.pipe, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)op.k.pipe_smem) != cudaSuccess))) {
         cudaGetLastError();
         fail("kernel shared memory configuration failed");
         return;
@@ -706,7 +726,13 @@ std::unique_ptr<Plan> build_plan(int kind, int ndim, const long long* dims, long
   P->ndim = ndim;
   for (int i = 0; i < ndim; i++) P->dims[i] = dims[i];
   P->batch = batch;
-  if (!dry) cudaGetDevice(&P->device);
+  if (!dry) {
+    cudaGetDevice(&P->device);
+    if (cudaDeviceGetAttribute(&P->sm_count, cudaDevAttrMultiProcessorCount, P->device) != cudaSuccess) {
+      cudaGetLastError();
+      P->sm_count = 0;   // the pipelined kernels stay off
+    }
+  }
 
   long long N = 1;
   for (int i = 0; i < ndim; i++) N *= dims[i];
@@ -903,11 +929,11 @@ std::string describe_plan(const Plan& P) {
     if (op.type == OP_LINE) {
       snprintf(buf, sizeof buf,
                "{\"type\":\"line\",\"logl\":%d,\"cols\":%d,\"lk\":%d,\"tstore\":%d,\"tc\":%d,\"C\":%d,"
-               "\"halves\":%d,\"unit\":%d,\"tma\":%d,"
+               "\"halves\":%d,\"unit\":%d,\"tma\":%d,\"pipe\":%d,"
                "\"threads\":%d,\"smem\":%zu,\"grid\":%lld,\"nlines\":%lld,\"inverse\":%d,"
                "\"tw_n\":%lld,\"tw_qmask\":%lld,\"tw_qshift\":%d,\"real_L\":%lld,\"pcols\":%lld,",
                op.k.logl, op.k.cols, op.k.kind, op.k.tstore, op.k.tc, op.k.lines_per_cta, op.k.halves, op.k.unit,
-               op.k.tma != nullptr, op.threads,
+               op.k.tma != nullptr, op.k.pipe != nullptr, op.threads,
                op.smem,
                op.grid, op.p.nlines, op.p.inverse, op.p.tw_n, op.p.tw_qmask, op.p.tw_qshift, op.real_L, op.p.pcols);
     } else if (op.type == OP_REAL) {
@@ -1043,7 +1069,11 @@ int Plan::launch(const float* src_re, const float* src_im, float* dst_re, float*
       p.in = bind(op.in, base, esz);
       p.out = bind(op.out, base, esz);
       TmaTile tm;
-      if (op.k.tma && tma_tile(p, op.k, &tm)) {
+      if (op.k.pipe && sm_count > 0 && tma_tile(p, op.k, &tm)) {
+        // persistent: at most one CTA per SM, each walking tiles gridDim.x apart
+        const long long g = std::min<long long>(op.grid, sm_count);
+        op.k.pipe<<<(unsigned)g, op.threads, op.k.pipe_smem, st>>>(p, tm, op.grid);
+      } else if (op.k.tma && tma_tile(p, op.k, &tm)) {
         op.k.tma<<<(unsigned)op.grid, op.threads, op.smem, st>>>(p, tm);
       } else {
         op.k.fn<<<(unsigned)op.grid, op.threads, op.smem, st>>>(p);

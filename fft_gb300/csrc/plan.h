@@ -68,6 +68,7 @@ struct Plan {
   long long in_elems = 0;      // complex (or real) elements per array, one transform
   long long out_elems = 0;
   int device = 0;
+  int sm_count = 0;            // SMs of the device (the pipelined kernels' grid bound)
   std::vector<Op> ops;
   long long scratch_elems = 0;   // scratch elements (floats, doubles in FP64 plans)
   long long real_L_of_op = 0;
@@ -107,6 +108,8 @@ struct Tuning {
   int cols_c = 0;     // lines per CTA of the 256- and 512-point complex cols passes (0: the default)
   int passes = 0;     // 1D complex axes of 2^20 points and more: 0 the built-in rule (three passes
                       // from 2^21), 2 two passes, 3 three passes
+  int no_pipe = 0;    // 1: 2048-point cols passes keep their one-tile-per-CTA kernels (the queue's
+                      // grouped launches have no pipelined form)
 };
 // The tuned choice for a shape on the current device, if the autotuner has
 // one (tuning it first when AFFT_GB300_AUTOTUNE=1); else the defaults.

@@ -110,9 +110,12 @@ static int build_queue(QueueImpl& Q) {
     key.insert(key.end(), dims, dims + nd);
     auto it = Q.plans.find(key);
     if (it == Q.plans.end()) {
-      Tuning tq;
-      if (Q.tuned) tq = tuned_for_queue(d.kind, nd, dims);
-      auto P = build_plan(d.kind, nd, dims, 1, 0, false, Q.form, Q.tuned ? &tq : nullptr);
+      // the tuned choice (for queues created with it), else what a plan of
+      // this shape gets; grouped launches have no pipelined form
+      Tuning tq = Q.tuned ? tuned_for_queue(d.kind, nd, dims)
+                          : (Q.form == 0 ? tuned_choice(d.kind, nd, dims, 1, 0) : Tuning{});
+      tq.no_pipe = 1;
+      auto P = build_plan(d.kind, nd, dims, 1, 0, false, Q.form, &tq);
       if (!P) return AFFT_GB300_EINVAL;
       it = Q.plans.emplace(key, std::shared_ptr<Plan>(P.release())).first;
     }

@@ -134,10 +134,11 @@ void save_locked(const TuneCache& C) {
 // what distinguishes two built variants: the kernels they launch and how
 std::string signature(const Plan& P) {
   std::string s;
-  char buf[128];
+  char buf[160];
   for (const Op& op : P.ops) {
-    snprintf(buf, sizeof buf, "%d:%p:%p:%d:%d:%d:%lld;", op.type, op.type == OP_LINE ? (const void*)op.k.fn : nullptr,
-             op.type == OP_LINE ? (const void*)op.k.tma : nullptr, op.k.logl, op.k.lines_per_cta, op.k.tc,
+    snprintf(buf, sizeof buf, "%d:%p:%p:%p:%d:%d:%d:%lld;", op.type,
+             op.type == OP_LINE ? (const void*)op.k.fn : nullptr, op.type == OP_LINE ? (const void*)op.k.tma : nullptr,
+             op.type == OP_LINE ? (const void*)op.k.pipe : nullptr, op.k.logl, op.k.lines_per_cta, op.k.tc,
              op.type == OP_LINE ? op.p.nlines : op.rp.nlines);
     s += buf;
   }

@@ -198,18 +198,19 @@ def test_long_real_scratch_is_pairs():
 
 
 @pytest.mark.parametrize("kind,dims,batch,expect", [
-    ("c", [256, 256, 256], 1, [0, 1, 1]),        # rows, then two 256-point cols passes by TMA
-    ("c", [65536], 64, [1, 1]),                  # four-step: pass A (transposing store) and pass B by TMA
-    ("c", [1024, 1024], 4, [0, 1]),              # 1024-point cols pass by TMA
-    ("ri", [4096, 4096], 1, [0, 1]),             # the 2048-point C2R pass by TMA
-    ("r", [4096, 4096], 1, [0, 0]),              # the split 2048-point R2C pass keeps LSU loads (measured)
-    ("c", [2048, 2048], 2, [0, 0]),              # the 2048-point C2C pass keeps LSU loads (measured)
-    ("c", [4096], 64, [0]),                      # rows passes load through the LSU
+    ("c", [256, 256, 256], 1, [(0, 0), (1, 0), (1, 0)]),   # rows, then two 256-point cols passes by TMA
+    ("c", [65536], 64, [(1, 0), (1, 0)]),                  # four-step: pass A (transposing store) and pass B by TMA
+    ("c", [1024, 1024], 4, [(0, 0), (1, 0)]),              # 1024-point cols pass by TMA
+    ("ri", [4096, 4096], 1, [(0, 0), (1, 1)]),             # the 2048-point C2R pass pipelined
+    ("r", [4096, 4096], 1, [(0, 0), (0, 0)]),              # the split 2048-point R2C pass keeps LSU loads (measured)
+    ("c", [2048, 2048], 2, [(0, 0), (1, 1)]),              # the 2048-point C2C cols pass pipelined
+    ("c", [4096], 64, [(0, 0)]),                           # rows passes load through the LSU
 ], ids=str)
 def test_tma_fed_passes(kind, dims, batch, expect):
-    """Which passes take the TMA-fed cols kernels (the plan's default choice;
-    at launch the LSU kernel of the same shape runs instead where the bound
-    arrays miss the TMA alignment rules)."""
+    """Which passes take the TMA-fed cols kernels, as (tma, pipe): the plan's
+    default choice.  pipe: the persistent pipelined form of the 2048-point
+    cols passes.  At launch the LSU kernel of the same shape runs instead
+    where the bound arrays miss the TMA alignment rules."""
     d = describe(kind, dims, batch)
-    got = [op.get("tma", 0) for op in d["ops"] if op["type"] == "line"]
+    got = [(op.get("tma", 0), op.get("pipe", 0)) for op in d["ops"] if op["type"] == "line"]
     assert got == expect, (got, d["ops"])
