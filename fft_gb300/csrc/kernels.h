@@ -9,7 +9,7 @@ namespace agb {
 typedef void (*LineKernelFn)(LineParams);
 typedef void (*GroupedKernelFn)(const Segment*, const int*, long long);
 typedef void (*LineKernelTmaFn)(LineParams, TmaTile);
-typedef void (*LineKernelPipeFn)(LineParams, TmaTile, long long);
+typedef void (*LineKernelPipeFn)(LineParams, TmaTile, TmaTile, long long);
 
 struct LineKernel {
   LineKernelFn fn;

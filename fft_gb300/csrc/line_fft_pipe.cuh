@@ -7,7 +7,8 @@
 // blockIdx.x + gridDim.x, ...  As soon as its threads have taken tile i out
 // of the raw buffer (into registers), one thread issues the TMA loads of the
 // CTA's next tile into that buffer.  Those land while tile i's stages run and
-// its results are stored.
+// its results are stored (the C2C pass: by TMA from the exchange buffer, one
+// plane at a time).
 //
 // Shared memory: the raw tile ([re: L rows x C][im: L rows x C] floats,
 // 128 KB, as tma_load_tile lays it out) and a separate exchange buffer through
@@ -25,7 +26,26 @@
 #pragma once
 #include "line_fft.cuh"
 
+// LATE_ISSUE: the next tile's loads go out after the first exchange barrier
+// (which then also marks the raw tile consumed) instead of after a barrier of
+// their own: 1% faster for C2R, and for C2C with BULK_STORE.  BULK_STORE: the
+// C2C pass stages each output plane in the exchange buffer and stores it with
+// TMA (cp.async.bulk.tensor) instead of per-thread stores: 1-3% faster for
+// C2C, 1-2.5% slower for C2R (which keeps per-thread stores).
+#ifndef AFFT_PIPE_LATE_ISSUE
+#define AFFT_PIPE_LATE_ISSUE 1
+#endif
+#ifndef AFFT_PIPE_BULK_STORE
+#define AFFT_PIPE_BULK_STORE 1
+#endif
+
 namespace agb {
+
+// the passes that store by TMA
+template <int KIND>
+constexpr bool pipe_bulk() {
+  return AFFT_PIPE_BULK_STORE && KIND == LK_C2C;
+}
 
 // Rows of the exchange buffer for the 2048-point schedule (radix 8, 16, 16;
 // T = 128, E = 16).  Stage 0 scatters output e = u + 2 r of butterfly
@@ -48,8 +68,9 @@ __device__ __forceinline__ int pipe_row(int j) { return j + (j >> 3); }
 // The exchange after stage S: every value to its stage-S position, then
 // element t + T e of this thread's line back, re parts first, then im parts.
 // TRAIL: the buffer is written again before the next CTA-wide barrier.
-template <int LOGL, int C, int S, bool TRAIL>
-__device__ __forceinline__ void pipe_exchange(float2 (&v)[Sched<LOGL>::E], int t, int c, float* xs) {
+// hook: run by every thread after the first barrier (the late tile issue).
+template <int LOGL, int C, int S, bool TRAIL, class Hook>
+__device__ __forceinline__ void pipe_exchange(float2 (&v)[Sched<LOGL>::E], int t, int c, float* xs, const Hook& hook) {
   constexpr int E = Sched<LOGL>::E;
   float* w = xs + pipe_wbase<S>(t) * C + c;
   const float* g = xs + pipe_gbase(t) * C + c;
@@ -57,6 +78,7 @@ __device__ __forceinline__ void pipe_exchange(float2 (&v)[Sched<LOGL>::E], int t
 #pragma unroll
   for (int e = 0; e < E; e++) w[pipe_woff<S>(e) * C] = v[e].x;
   __syncthreads();
+  hook();
 #pragma unroll
   for (int e = 0; e < E; e++) nx[e] = g[pipe_goff(e) * C];
   __syncthreads();
@@ -70,9 +92,9 @@ __device__ __forceinline__ void pipe_exchange(float2 (&v)[Sched<LOGL>::E], int t
 
 // All stages of one tile, values in registers in the canonical layout on
 // entry and exit (as run_stages).
-template <int LOGL, int C, int KIND, int S>
+template <int LOGL, int C, int KIND, int S, class Hook>
 __device__ __forceinline__ void pipe_stages(float2 (&v)[Sched<LOGL>::E], int t, int c, const float2* tw,
-                                            float* xs) {
+                                            float* xs, const Hook& hook) {
   using Sc = Sched<LOGL>;
   if constexpr (S < Sc::NSTAGES) {
     constexpr int R = Sc::radix(S), NS = Sc::ns(S);
@@ -80,8 +102,13 @@ __device__ __forceinline__ void pipe_stages(float2 (&v)[Sched<LOGL>::E], int t, 
     stage<R, NS, Sc::E, Sc::T, true, false, 0, packed_bfly<LOGL, true>()>(v, t, c, tw + Sc::twoff(S), xs, false,
                                                                          nullptr);
     if constexpr (S + 1 < Sc::NSTAGES) {
-      pipe_exchange<LOGL, C, S, (S + 2 < Sc::NSTAGES || KIND == LK_R2C)>(v, t, c, xs);
-      pipe_stages<LOGL, C, KIND, S + 1>(v, t, c, tw, xs);
+      constexpr bool TRAIL = S + 2 < Sc::NSTAGES || KIND == LK_R2C || pipe_bulk<KIND>();
+      if constexpr (S == 0) {
+        pipe_exchange<LOGL, C, S, TRAIL>(v, t, c, xs, hook);
+      } else {
+        pipe_exchange<LOGL, C, S, TRAIL>(v, t, c, xs, [] {});
+      }
+      pipe_stages<LOGL, C, KIND, S + 1>(v, t, c, tw, xs, hook);
     }
   }
 }
@@ -102,13 +129,33 @@ __device__ __forceinline__ void pipe_issue(const LineParams& p, const TmaTile& t
   }
 }
 
+__device__ __forceinline__ void tma_store_3d(const CUtensorMap* map, int x, int y, int z, uint32_t src) {
+  asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%1, %2, %3}], [%4];" ::"l"(
+                   reinterpret_cast<uint64_t>(map)),
+               "r"(x), "r"(y), "r"(z), "r"(src)
+               : "memory");
+}
+
+// Store one output plane of tile `tile` from the dense [L][C] staging in the
+// exchange buffer (boxes of C columns x box_rows rows), as one bulk group.
+template <int L, int C>
+__device__ __forceinline__ void pipe_store_plane(const LineParams& p, const CUtensorMap* map, int box_rows,
+                                                 long long tile, uint32_t xs) {
+  const long long q0 = tile * C;
+  const int col = (int)(q0 & p.out.qmask);
+  const int outer = (int)(q0 >> p.out.qshift);
+  for (int r = 0; r < L; r += box_rows) tma_store_3d(map, col, r, outer, xs + (uint32_t)r * C * 4u);
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+
 // KIND: LK_C2C (with the four-step twiddle when p.tw_n), LK_R2C (unsplit:
 // the post-pass through the exchange buffer), LK_C2R (the pre-pass from the
 // raw tile, bin L read directly).  Split planes in, split planes out; every
 // tile whole (the host's tma_tile rules).  ntiles = nlines / C.
 template <int LOGL, int C, int KIND>
 __global__ void __launch_bounds__(Sched<LOGL>::T * C, 1)
-line_fft_pipe(const LineParams p, const __grid_constant__ TmaTile tm, long long ntiles) {
+line_fft_pipe(const LineParams p, const __grid_constant__ TmaTile tm, const __grid_constant__ TmaTile tmo,
+              long long ntiles) {
   using Sc = Sched<LOGL>;
   constexpr int L = Sc::L, E = Sc::E, T = Sc::T;
   static_assert(KIND == LK_C2C || KIND == LK_R2C || KIND == LK_C2R, "plain cols kinds");
@@ -122,6 +169,7 @@ line_fft_pipe(const LineParams p, const __grid_constant__ TmaTile tm, long long 
   const int c = tid % C, t = tid / C;
   const uint32_t mb = smem_u32(&mbar);
   const uint32_t raw_s = smem_u32(raw);
+  constexpr bool BULK = pipe_bulk<KIND>();
 
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb));
@@ -133,6 +181,9 @@ line_fft_pipe(const LineParams p, const __grid_constant__ TmaTile tm, long long 
 
   uint32_t phase = 0;
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, phase ^= 1u) {
+    // the previous tile's bulk stores have read the exchange buffer before
+    // anyone writes it again
+    if (BULK && tid == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
     if (!__syncthreads_and(tc_wait(mb, phase))) {
       if (tid == 0) {
         if (p.err) atomicExch(p.err, 2);
@@ -182,13 +233,19 @@ line_fft_pipe(const LineParams p, const __grid_constant__ TmaTile tm, long long 
       }
     }
     // every thread has its tile: the raw buffer takes the next one
-    __syncthreads();
-    if (tid == 0 && tile + gridDim.x < ntiles) {
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      pipe_issue<L, C>(p, tm, tile + gridDim.x, raw_s, mb);
+    auto issue_next = [&] {
+      if (tid == 0 && tile + gridDim.x < ntiles) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        pipe_issue<L, C>(p, tm, tile + gridDim.x, raw_s, mb);
+      }
+    };
+    if constexpr (AFFT_PIPE_LATE_ISSUE) {
+      pipe_stages<LOGL, C, KIND, 0>(v, t, c, p.tw, xs, issue_next);
+    } else {
+      __syncthreads();
+      issue_next();
+      pipe_stages<LOGL, C, KIND, 0>(v, t, c, p.tw, xs, [] {});
     }
-
-    pipe_stages<LOGL, C, KIND, 0>(v, t, c, p.tw, xs);
 
     const long long base = line_off(p.out, q);
     const long long S = (long long)T * p.out.es;
@@ -206,16 +263,34 @@ line_fft_pipe(const LineParams p, const __grid_constant__ TmaTile tm, long long 
 #pragma unroll
         for (int e = 0; e < E; e++) v[e] = cswap(v[e]);
       }
+    } else if constexpr (KIND == LK_C2R) {
+#pragma unroll
+      for (int e = 0; e < E; e++) v[e] = cswap(v[e]);   // re of the output is im of the swapped transform
+    }
+    if constexpr (BULK) {
+      // each plane through the exchange buffer, dense [L][C] as the boxes
+      // lay it out (a warp writes 32 consecutive words)
+      float* st = xs + t * C + c;
+      const uint32_t xs_s = smem_u32(xs);
+#pragma unroll
+      for (int e = 0; e < E; e++) st[e * T * C] = v[e].x;
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncthreads();
+      if (tid == 0) {
+        pipe_store_plane<L, C>(p, &tmo.re, tmo.box_rows, tile, xs_s);
+        asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+      }
+      __syncthreads();
+#pragma unroll
+      for (int e = 0; e < E; e++) st[e * T * C] = v[e].y;
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncthreads();
+      if (tid == 0) pipe_store_plane<L, C>(p, &tmo.im, tmo.box_rows, tile, xs_s);
+    } else if constexpr (KIND == LK_C2C || KIND == LK_C2R) {
 #pragma unroll
       for (int e = 0; e < E; e++) {
         pr[e * S] = v[e].x;
         pi[e * S] = v[e].y;
-      }
-    } else if constexpr (KIND == LK_C2R) {
-#pragma unroll
-      for (int e = 0; e < E; e++) {
-        pr[e * S] = v[e].y;   // swapped back: re of the output is im of the swapped transform
-        pi[e * S] = v[e].x;
       }
     } else {
       // real forward post-pass (onedim.hpp:1058-1108 / multi.hpp:354-414):
@@ -254,6 +329,8 @@ line_fft_pipe(const LineParams p, const __grid_constant__ TmaTile tm, long long 
       }
     }
   }
+  // the last tile's bulk stores have read shared memory before the CTA ends
+  if (BULK && tid == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
 }
 
 }  // namespace agb

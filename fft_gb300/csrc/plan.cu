@@ -997,26 +997,21 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   return fn;
 }
 
-// The tensor maps of a cols pass's input planes, when the bound arrays
-// allow them: lines are whole tiles of C adjacent columns of one outer block
-// (lo = 1, ncols = 2^qshift a multiple of C, every block whole), both plane
-// bases 16-byte aligned, row and block strides multiples of 16 bytes.  Boxes
-// of C columns x min(L, 256) rows.  false: launch the LSU kernel instead.
-bool tma_tile(const LineParams& p, const LineKernel& k, TmaTile* tm) {
-  const LineIO& in = p.in;
-  const long long L = 1LL << k.logl, C = k.lines_per_cta;
-  const long long ncols = in.qmask + 1;
-  // input pairs (cols kernels with pairs bit 0): one interleaved array,
-  // adjacent columns adjacent pairs
-  const bool pairs = (k.unit & 1) != 0;
-  if (in.lo != (pairs ? 2 : 1) || ncols != (1LL << in.qshift) || ncols % C || p.nlines % ncols ||
-      L > (1LL << 16))
+// The tensor maps of one side (input or output planes) of a cols pass, when
+// the bound arrays allow them: lines are whole tiles of C adjacent columns of
+// one outer block (lo = 1, ncols = 2^qshift a multiple of C, every block
+// whole), both plane bases 16-byte aligned, row and block strides multiples
+// of 16 bytes.  Boxes of C columns x min(L, 256) rows.
+static bool encode_tile(const LineIO& io, long long nlines, long long L, long long C, bool pairs, TmaTile* tm) {
+  const long long ncols = io.qmask + 1;
+  // pairs: one interleaved array, adjacent columns adjacent pairs
+  if (io.lo != (pairs ? 2 : 1) || ncols != (1LL << io.qshift) || ncols % C || nlines % ncols || L > (1LL << 16))
     return false;
-  if (pairs ? (in.im != in.re + 1 || (reinterpret_cast<uintptr_t>(in.re) & 15))
-            : ((reinterpret_cast<uintptr_t>(in.re) | reinterpret_cast<uintptr_t>(in.im)) & 15))
+  if (pairs ? (io.im != io.re + 1 || (reinterpret_cast<uintptr_t>(io.re) & 15))
+            : ((reinterpret_cast<uintptr_t>(io.re) | reinterpret_cast<uintptr_t>(io.im)) & 15))
     return false;
-  const long long nouter = p.nlines / ncols;
-  const long long rs = in.es * 4, bs = nouter > 1 ? in.hi * 4 : L * in.es * 4;
+  const long long nouter = nlines / ncols;
+  const long long rs = io.es * 4, bs = nouter > 1 ? io.hi * 4 : L * io.es * 4;
   if (rs % 16 || bs % 16 || rs <= 0 || bs <= 0 || rs >= (1LL << 40) || bs >= (1LL << 40)) return false;
   auto encode = tensor_map_encoder();
   if (!encode) return false;
@@ -1026,7 +1021,7 @@ bool tma_tile(const LineParams& p, const LineKernel& k, TmaTile* tm) {
   const cuuint32_t box[3] = {(cuuint32_t)(pairs ? 2 * C : C), (cuuint32_t)br, 1};
   const cuuint32_t estr[3] = {1, 1, 1};
   for (int i = 0; i < (pairs ? 1 : 2); i++) {
-    if (encode(i ? &tm->im : &tm->re, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)(i ? in.im : in.re), dims, strides,
+    if (encode(i ? &tm->im : &tm->re, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)(i ? io.im : io.re), dims, strides,
                box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
       return false;
@@ -1036,6 +1031,17 @@ bool tma_tile(const LineParams& p, const LineKernel& k, TmaTile* tm) {
   tm->rows = (int)L;
   tm->pairs = pairs ? 1 : 0;
   return true;
+}
+
+// The input planes' maps (false: launch the LSU kernel instead).  Input
+// pairs for cols kernels with pairs bit 0.
+bool tma_tile(const LineParams& p, const LineKernel& k, TmaTile* tm) {
+  return encode_tile(p.in, p.nlines, 1LL << k.logl, k.lines_per_cta, (k.unit & 1) != 0, tm);
+}
+
+// The output planes' maps of a pipelined pass that stores by TMA.
+bool tma_tile_out(const LineParams& p, const LineKernel& k, TmaTile* tm) {
+  return encode_tile(p.out, p.nlines, 1LL << k.logl, k.lines_per_cta, false, tm);
 }
 
 bool op_tables_ok(const Op& op) {
@@ -1068,11 +1074,12 @@ int Plan::launch(const float* src_re, const float* src_im, float* dst_re, float*
       LineParams p = op.p;
       p.in = bind(op.in, base, esz);
       p.out = bind(op.out, base, esz);
-      TmaTile tm;
-      if (op.k.pipe && sm_count > 0 && tma_tile(p, op.k, &tm)) {
+      TmaTile tm, tmo{};
+      if (op.k.pipe && sm_count > 0 && tma_tile(p, op.k, &tm) &&
+          (!(AFFT_PIPE_BULK_STORE && op.k.kind == LK_C2C) || tma_tile_out(p, op.k, &tmo))) {
         // persistent: at most one CTA per SM, each walking tiles gridDim.x apart
         const long long g = std::min<long long>(op.grid, sm_count);
-        op.k.pipe<<<(unsigned)g, op.threads, op.k.pipe_smem, st>>>(p, tm, op.grid);
+        op.k.pipe<<<(unsigned)g, op.threads, op.k.pipe_smem, st>>>(p, tm, tmo, op.grid);
       } else if (op.k.tma && tma_tile(p, op.k, &tm)) {
         op.k.tma<<<(unsigned)op.grid, op.threads, op.smem, st>>>(p, tm);
       } else {
