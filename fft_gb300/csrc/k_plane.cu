@@ -1,0 +1,21 @@
+// plane-fused passes (plane_fft): planes of 2^12 .. 2^14 points, sides 32 .. 512
+#include "kernels.h"
+namespace agb {
+bool get_plane_kernel(int log1, int log2, LineKernel* out) {
+  switch (log1 * 16 + log2) {
+    case 5 * 16 + 7: *out = make_plane_kernel<5, 7>(); return true;
+    case 6 * 16 + 6: *out = make_plane_kernel<6, 6>(); return true;
+    case 7 * 16 + 5: *out = make_plane_kernel<7, 5>(); return true;
+    case 5 * 16 + 8: *out = make_plane_kernel<5, 8>(); return true;
+    case 6 * 16 + 7: *out = make_plane_kernel<6, 7>(); return true;
+    case 7 * 16 + 6: *out = make_plane_kernel<7, 6>(); return true;
+    case 8 * 16 + 5: *out = make_plane_kernel<8, 5>(); return true;
+    case 5 * 16 + 9: *out = make_plane_kernel<5, 9>(); return true;
+    case 6 * 16 + 8: *out = make_plane_kernel<6, 8>(); return true;
+    case 7 * 16 + 7: *out = make_plane_kernel<7, 7>(); return true;
+    case 8 * 16 + 6: *out = make_plane_kernel<8, 6>(); return true;
+    case 9 * 16 + 5: *out = make_plane_kernel<9, 5>(); return true;
+  }
+  return false;
+}
+}  // namespace agb

@@ -3,6 +3,7 @@
 #pragma once
 #include "line_fft.cuh"
 #include "line_fft_pipe.cuh"
+#include "plane_fft.cuh"
 
 namespace agb {
 
@@ -32,6 +33,8 @@ struct LineKernel {
   LineKernelPipeFn pipe = nullptr;   // the persistent TMA-pipelined form (line_fft_pipe), or null;
                                      // launched on at most one CTA per SM with the tile count
   size_t pipe_smem = 0;              // its dynamic shared memory (raw tile + exchange buffer)
+  int plane_log1 = 0;                // plane kernels (plane_fft): log2 of the rows per plane (the column
+                                     // axis); logl is then log2 of the row length; 0 for line kernels
 };
 
 constexpr int ROWS_MAX_LOG = 14;   // rows mode: one CTA up to 16384 points
@@ -83,6 +86,11 @@ bool get_cols_tma_pairs(int logl, bool tstore, int pairs, LineKernel* out);
 // persistent TMA-pipelined form (k_cols_pipe.cu): out->pipe set, out->tma and
 // out->fn the one-tile-per-CTA kernels of the same shape
 bool get_cols_pipe(int logl, int kind, LineKernel* out);
+
+// plane-fused passes (plane_fft.cuh, k_plane*.cu): the last two axes of a
+// complex N-D transform, planes of 2^log1 rows x 2^log2 points with
+// 12 <= log1 + log2 <= 14 and both in [5, 9]
+bool get_plane_kernel(int log1, int log2, LineKernel* out);
 
 // cols c2c passes (not transposing) with another tile width, for the
 // autotuner: 256 points in 8 or 32 lines, 512 points in 16; TMA-fed
@@ -168,6 +176,30 @@ LineKernel make_tma_kernel() {
   LineKernel k = make_line_kernel<LOGL, true, KIND, TSTORE, false, UNIT, C>();
   k.tma = &line_fft_tma<LOGL, C, KIND, TSTORE, UNIT>;
   k.grouped_tma = &line_fft_grouped<LOGL, C, true, KIND, TSTORE, false, UNIT, true>;
+  return k;
+}
+
+// a plane pass: one CTA per plane, D1 D2 / 16 threads
+template <int LOG1, int LOG2>
+LineKernel make_plane_kernel() {
+  using PS = PlaneShape<LOG1, LOG2>;
+  LineKernel k;
+  k.fn = &plane_fft<LOG1, LOG2>;
+  k.grouped = &plane_fft_grouped<LOG1, LOG2>;
+  k.tma = nullptr;
+  k.grouped_tma = nullptr;
+  k.logl = LOG2;
+  k.plane_log1 = LOG1;
+  k.cols = 0;
+  k.kind = LK_C2C;
+  k.tstore = 0;
+  k.tc = 0;
+  k.unit = 1;
+  k.lines_per_cta = PS::D1;   // rows per plane: the grid is one CTA per plane
+  k.threads = PS::NT;
+  k.smem = (size_t)PS::FLOAT2S * sizeof(float2);
+  k.halves = 1;
+  k.stage_logl = LOG2;
   return k;
 }
 

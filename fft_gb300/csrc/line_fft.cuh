@@ -88,6 +88,7 @@ struct LineParams {
   int inverse;              // swap re/im on load and store
   const __half* tc_b;       // TC form: Mh then Ml, 32x32 FP16 each, [n][k]
   int* err;                 // TC form: error word set when a bounded wait gives up
+  const float2* tw2;        // plane passes: stage twiddles of the column axis
 };
 
 // ---------------------------------------------------------------------------

@@ -390,6 +390,11 @@ static View inter_view(int b, long long off = 0) {  // re,im pairs in one array
 #ifndef AFFT_COLS_PIPE
 #define AFFT_COLS_PIPE 1
 #endif
+// the last two axes of complex N-D transforms in one plane-fused pass
+// (plane_fft) where a plane of 2^12 .. 2^14 points fits one CTA
+#ifndef AFFT_PLANE
+#define AFFT_PLANE 1
+#endif
 // the 2048-point R2C pass in that form too (unsplit), instead of the split
 // one-tile-per-two-CTAs form
 #ifndef AFFT_PIPE_R2C
@@ -573,6 +578,52 @@ struct Builder {
     P.ops.push_back(op);
   }
 
+  // Whether the last two axes (d1 rows of d2 points) of a complex N-D
+  // transform from A to B take one plane-fused pass: split planes, the
+  // shapes plane_fft is built for, FP32 plain form, not tuned off.
+  bool plane_fits(long long d1, long long d2, const View& A, const View& B) const {
+    if (!AFFT_PLANE || f64 || P.form == FORM_TC || tune.no_plane || A.unit != 1 || B.unit != 1) return false;
+    if (d1 < 2 || d2 < 2 || (d1 & (d1 - 1)) || (d2 & (d2 - 1))) return false;
+    LineKernel k;
+    return get_plane_kernel(ilog2ll(d1), ilog2ll(d2), &k);
+  }
+
+  // `count` dense planes of d1 rows x d2 points from A to B, one CTA each.
+  void plane(long long d1, long long d2, long long count, const View& A, const View& B, bool inverse) {
+    if (!ok) return;
+    Op op;
+    op.type = OP_LINE;
+    const int log1 = ilog2ll(d1), log2 = ilog2ll(d2);
+    if (!get_plane_kernel(log1, log2, &op.k)) {
+      fail("no plane kernel for this shape");
+      return;
+    }
+    const long long pl = d1 * d2;
+    op.in = io(A, 1, 0, pl, 0, 0);
+    op.out = io(B, 1, 0, pl, 0, 0);
+    op.p.nlines = count * d1;   // rows; the grid is one CTA per plane
+    op.p.inverse = inverse ? 1 : 0;
+    if (!dry) {
+      if (op.k.smem > 48 * 1024 &&
+          cudaFuncSetAttribute((const void*)op.k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)op.k.smem) !=
+              cudaSuccess) {
+        cudaGetLastError();
+        fail("kernel shared memory configuration failed");
+        return;
+      }
+      op.p.tw = stage_twiddles(log2);
+      op.p.tw2 = stage_twiddles(log1);
+      if (!op.p.tw || !op.p.tw2) {
+        fail("twiddle table allocation failed");
+        return;
+      }
+    }
+    op.grid = count;
+    op.threads = op.k.threads;
+    op.smem = op.k.smem;
+    P.ops.push_back(op);
+  }
+
   void real_pass(const IOSpec& in, const IOSpec& out, long long nlines, long long L, bool inverse,
                  bool lines_fastest) {
     if (!ok) return;
@@ -701,7 +752,14 @@ struct Builder {
     long long total = count;
     for (int i = 0; i < nd; i++) total *= dims[i];
     bool first = true;
-    for (int ax = nd - 1; ax >= 0; ax--) {
+    int ax0 = nd - 1;
+    if (nd >= 2 && plane_fits(dims[nd - 2], dims[nd - 1], A, B)) {
+      // the last two axes in one pass, then the others in place
+      plane(dims[nd - 2], dims[nd - 1], total / (dims[nd - 2] * dims[nd - 1]), A, B, inverse);
+      first = false;
+      ax0 = nd - 3;
+    }
+    for (int ax = ax0; ax >= 0; ax--) {
       long long L = dims[ax];
       if (L == 1) continue;
       long long inner = 1;
@@ -929,11 +987,11 @@ std::string describe_plan(const Plan& P) {
     if (op.type == OP_LINE) {
       snprintf(buf, sizeof buf,
                "{\"type\":\"line\",\"logl\":%d,\"cols\":%d,\"lk\":%d,\"tstore\":%d,\"tc\":%d,\"C\":%d,"
-               "\"halves\":%d,\"unit\":%d,\"tma\":%d,\"pipe\":%d,"
+               "\"halves\":%d,\"unit\":%d,\"tma\":%d,\"pipe\":%d,\"plane\":%d,"
                "\"threads\":%d,\"smem\":%zu,\"grid\":%lld,\"nlines\":%lld,\"inverse\":%d,"
                "\"tw_n\":%lld,\"tw_qmask\":%lld,\"tw_qshift\":%d,\"real_L\":%lld,\"pcols\":%lld,",
                op.k.logl, op.k.cols, op.k.kind, op.k.tstore, op.k.tc, op.k.lines_per_cta, op.k.halves, op.k.unit,
-               op.k.tma != nullptr, op.k.pipe != nullptr, op.threads,
+               op.k.tma != nullptr, op.k.pipe != nullptr, op.k.plane_log1, op.threads,
                op.smem,
                op.grid, op.p.nlines, op.p.inverse, op.p.tw_n, op.p.tw_qmask, op.p.tw_qshift, op.real_L, op.p.pcols);
     } else if (op.type == OP_REAL) {
@@ -1047,7 +1105,8 @@ bool tma_tile_out(const LineParams& p, const LineKernel& k, TmaTile* tm) {
 bool op_tables_ok(const Op& op) {
   if (op.type != OP_LINE) return op.type != OP_REAL || op.rp.rtw;
   return op.p.tw && (op.k.kind == LK_C2C || op.p.rtw) &&
-         (!op.p.tw_n || op.p.tw_full || (op.p.tw_hi && op.p.tw_lo)) && (!op.k.tc || op.p.tc_b);
+         (!op.p.tw_n || op.p.tw_full || (op.p.tw_hi && op.p.tw_lo)) && (!op.k.tc || op.p.tc_b) &&
+         (!op.k.plane_log1 || op.p.tw2);
 }
 
 int Plan::launch(const float* src_re, const float* src_im, float* dst_re, float* dst_im, cudaStream_t st) {

@@ -11,7 +11,9 @@ from plan_emulator import describe, run
 
 SHAPES = [[1], [2], [4], [16], [32], [256], [4096], [16384], [32768], [1 << 16], [1 << 19], [1 << 20], [1 << 21],
           [2, 2], [4, 8], [64, 4], [8, 4096], [4096, 8], [16, 2048, 2], [8192, 4], [2, 16384],
-          [2, 4, 8], [16, 16, 16], [4, 4, 4, 4], [2, 2, 2, 2, 2], [1, 32, 1], [4, 1, 1, 8]]
+          [2, 4, 8], [16, 16, 16], [4, 4, 4, 4], [2, 2, 2, 2, 2], [1, 32, 1], [4, 1, 1, 8],
+          # plane-fused last two axes (2^12 .. 2^14-point planes)
+          [4, 64, 64], [32, 128], [2, 256, 32], [2, 2, 32, 512]]
 
 
 def _inputs(kind, dims, batch, seed):
