@@ -192,7 +192,7 @@ def tune(kind, dims, batch=1, fmt=afft_split):
     L = lib()
     k = KINDS[kind] if isinstance(kind, str) else kind
     arr, n = _dims(dims)
-    buf = ctypes.create_string_buffer(8192)
+    buf = ctypes.create_string_buffer(65536)
     if L.afft_gb300_tune(k, n, arr, batch, fmt, buf, len(buf)):
         _check("tune")
         raise AfftError("tune failed")

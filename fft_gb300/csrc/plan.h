@@ -110,8 +110,8 @@ struct Tuning {
                       // from 2^21), 2 two passes, 3 three passes
   int no_pipe = 0;    // 1: 2048-point cols passes keep their one-tile-per-CTA kernels (the queue's
                       // grouped launches have no pipelined form)
-  int no_plane = 0;   // 1: the last two axes of complex N-D transforms take a pass each even where a
-                      // plane-fused pass applies
+  int no_plane = 0;   // the last two axes of complex N-D transforms where a plane-fused pass applies:
+                      // 0 the built-in rule, 1 a pass each, 2 the plane pass at any plane count
 };
 // The tuned choice for a shape on the current device, if the autotuner has
 // one (tuning it first when AFFT_GB300_AUTOTUNE=1); else the defaults.

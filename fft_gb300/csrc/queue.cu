@@ -115,6 +115,7 @@ static int build_queue(QueueImpl& Q) {
       Tuning tq = Q.tuned ? tuned_for_queue(d.kind, nd, dims)
                           : (Q.form == 0 ? tuned_choice(d.kind, nd, dims, 1, 0) : Tuning{});
       tq.no_pipe = 1;
+      if (tq.no_plane == 0) tq.no_plane = 2;   // one grouped launch gathers the planes of every transform
       auto P = build_plan(d.kind, nd, dims, 1, 0, false, Q.form, &tq);
       if (!P) return AFFT_GB300_EINVAL;
       it = Q.plans.emplace(key, std::shared_ptr<Plan>(P.release())).first;

@@ -11,7 +11,10 @@
 //  - the tile width (lines per CTA) of 256- and 512-point complex cols passes;
 //  - the plain FP32 form or the split-precision tensor-core form of the
 //    passes that have one;
-//  - 1D complex axes of 2^20 to 2^22 points in two passes or three.
+//  - 1D complex axes of 2^20 to 2^22 points in two passes or three;
+//  - the last two axes of complex N-D transforms in one plane-fused pass or
+//    one pass each (fusion depth; no_plane 0 the rule, 1 per axis, 2 fused
+//    at any plane count).
 // Each distinct variant (distinct kernels or launch shapes) is built as a
 // device plan and timed with CUDA events on zeroed buffers of the current
 // device (2 warm-up and 5 timed launches, median).  Choices live in a
@@ -79,9 +82,10 @@ std::string key_of(int kind, int ndim, const long long* dims, long long batch, i
 }
 
 // file format: a JSON object, one entry per line:
-//   "<key>": {"split": S, "real_inv": R, "cols_lsu": U, "tc": T, "cols_c": C, "passes": P, "ms": M},
-// (entries of the older forms, without passes or cols_lsu / tc / cols_c,
-// still load)
+//   "<key>": {"split": S, "real_inv": R, "cols_lsu": U, "tc": T, "cols_c": C, "passes": P,
+//             "no_plane": N, "ms": M},
+// (entries of the older forms, without no_plane, passes or cols_lsu / tc /
+// cols_c, still load)
 void load_locked(TuneCache& C) {
   if (C.loaded) return;
   C.loaded = true;
@@ -98,6 +102,11 @@ void load_locked(TuneCache& C) {
     if (!b) continue;
     Entry e;
     if (std::sscanf(b + 1,
+                    " : {\"split\": %d, \"real_inv\": %d, \"cols_lsu\": %d, \"tc\": %d, \"cols_c\": %d, "
+                    "\"passes\": %d, \"no_plane\": %d, \"ms\": %lf",
+                    &e.t.split, &e.t.real_inv, &e.t.cols_lsu, &e.t.tc, &e.t.cols_c, &e.t.passes, &e.t.no_plane,
+                    &e.ms) == 8 ||
+        std::sscanf(b + 1,
                     " : {\"split\": %d, \"real_inv\": %d, \"cols_lsu\": %d, \"tc\": %d, \"cols_c\": %d, "
                     "\"passes\": %d, \"ms\": %lf",
                     &e.t.split, &e.t.real_inv, &e.t.cols_lsu, &e.t.tc, &e.t.cols_c, &e.t.passes, &e.ms) == 7 ||
@@ -122,8 +131,8 @@ void save_locked(const TuneCache& C) {
     const Tuning& t = kv.second.t;
     std::fprintf(f,
                  "\"%s\": {\"split\": %d, \"real_inv\": %d, \"cols_lsu\": %d, \"tc\": %d, \"cols_c\": %d, "
-                 "\"passes\": %d, \"ms\": %.6f}%s\n",
-                 kv.first.c_str(), t.split, t.real_inv, t.cols_lsu, t.tc, t.cols_c, t.passes, kv.second.ms,
+                 "\"passes\": %d, \"no_plane\": %d, \"ms\": %.6f}%s\n",
+                 kv.first.c_str(), t.split, t.real_inv, t.cols_lsu, t.tc, t.cols_c, t.passes, t.no_plane, kv.second.ms,
                  ++i < C.table.size() ? "," : "");
   }
   std::fprintf(f, "}\n");
@@ -193,12 +202,18 @@ int tune_shape(int kind, int ndim, const long long* dims, long long batch, int f
   for (int i = 0; i < ndim; i++) maxdim = std::max(maxdim, dims[i]);
   static const int pass_forms[] = {0, 2, 3};
   const int npass = maxdim >= (1LL << 20) ? 3 : 1;
+  // plane-fused or per-axis last two axes, only for N-D shapes
+  // (innermost, so that the plain form's per-axis plan is recorded as
+  // no_plane = 1 before the tensor-core form, which has no plane pass,
+  // builds the same launches)
+  const int nplane = ndim >= 2 ? 3 : 1;
   for (int pf = 0; pf < npass; pf++)
   for (int split = 0; split < 2; split++)
     for (int real_inv = 0; real_inv < 2; real_inv++)
       for (int lsu = 0; lsu < 2; lsu++)
         for (int tc = 0; tc < 2; tc++)
-          for (int w : widths) {
+          for (int w : widths)
+          for (int np = 0; np < nplane; np++) {
             Tuning t;
             t.split = split;
             t.real_inv = real_inv;
@@ -206,6 +221,7 @@ int tune_shape(int kind, int ndim, const long long* dims, long long batch, int f
             t.tc = tc;
             t.cols_c = w;
             t.passes = pass_forms[pf];
+            t.no_plane = np;
             auto P = build_plan(kind, ndim, dims, batch, format, false, 0, &t);
             if (!P) {
               clear_error();
@@ -257,16 +273,16 @@ int tune_shape(int kind, int ndim, const long long* dims, long long batch, int f
       const Tuning& t = cands[i].first;
       snprintf(buf, sizeof buf,
                "%s{\"split\":%d,\"real_inv\":%d,\"cols_lsu\":%d,\"tc\":%d,\"cols_c\":%d,\"passes\":%d,"
-               "\"launches\":%zu,\"ms\":%.6f}",
-               i ? "," : "", t.split, t.real_inv, t.cols_lsu, t.tc, t.cols_c, t.passes, cands[i].second->ops.size(),
-               times[i]);
+               "\"no_plane\":%d,\"launches\":%zu,\"ms\":%.6f}",
+               i ? "," : "", t.split, t.real_inv, t.cols_lsu, t.tc, t.cols_c, t.passes, t.no_plane,
+               cands[i].second->ops.size(), times[i]);
       *report += buf;
     }
     const Tuning& t = out->t;
     snprintf(buf, sizeof buf,
              "],\"chosen\":{\"split\":%d,\"real_inv\":%d,\"cols_lsu\":%d,\"tc\":%d,\"cols_c\":%d,\"passes\":%d,"
-             "\"ms\":%.6f}}",
-             t.split, t.real_inv, t.cols_lsu, t.tc, t.cols_c, t.passes, out->ms);
+             "\"no_plane\":%d,\"ms\":%.6f}}",
+             t.split, t.real_inv, t.cols_lsu, t.tc, t.cols_c, t.passes, t.no_plane, out->ms);
     *report += buf;
   }
   return 0;

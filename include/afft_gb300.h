@@ -233,7 +233,9 @@ AFFT_GB300_API size_t afft_gb300_plan_describe(int kind, size_t ndim,
  * on its own; cols passes loading their tiles by TMA or through the LSU;
  * 8, 16 or 32 lines per CTA for 256- and 512-point complex cols passes; the
  * plain FP32 or the split-precision tensor-core form of the passes that have
- * one; and 1D complex axes of 2^20 to 2^22 points in two passes or three.  It allocates scratch device buffers for the timing.
+ * one; 1D complex axes of 2^20 to 2^22 points in two passes or three; and the
+ * last two axes of complex N-D transforms in one plane-fused pass or one pass
+ * each.  It allocates scratch device buffers for the timing.
  * Choices are kept for the process and, when the environment variable
  * AFFT_GB300_TUNE_CACHE names a file, stored there and reloaded on first use;
  * with AFFT_GB300_AUTOTUNE=1 every new shape is tuned when its first plan is

@@ -57,19 +57,21 @@ def _planes_of(kind, dims, batch=1):
 @pytest.mark.parametrize("kind", ["c", "ci"])
 def test_plane_2d(dev, kind, lg):
     dims = [1 << lg[0], 1 << lg[1]]
-    assert _planes_of(kind, dims) == [lg[0]]           # one plane pass is the whole transform
+    # (2^14-point planes take the plane pass from 256 planes per launch)
+    batch = 256 if lg[0] + lg[1] == 14 else 3
+    assert _planes_of(kind, dims, batch) == [lg[0]]           # one plane pass is the whole transform
     for inplace in (False, True):
-        got, ref = _batch(kind, dims, 3, dev, inplace=inplace, seed=lg[0] * 16 + lg[1])
+        got, ref = _batch(kind, dims, batch, dev, inplace=inplace, seed=lg[0] * 16 + lg[1])
         assert O.rel_l2(got, ref) <= TOL, (kind, dims, inplace)
 
 
 @pytest.mark.parametrize("kind", ["c", "ci"])
-@pytest.mark.parametrize("dims", [[8, 64, 64], [4, 32, 128], [4, 128, 128], [2, 256, 32], [8, 32, 512],
-                                  [2, 4, 64, 64]], ids=str)
-def test_plane_nd(dev, kind, dims):
+@pytest.mark.parametrize("dims,batch", [([8, 64, 64], 2), ([4, 32, 128], 2), ([16, 128, 128], 16), ([2, 256, 32], 2),
+                                        ([8, 32, 512], 32), ([2, 4, 64, 64], 2)], ids=str)
+def test_plane_nd(dev, kind, dims, batch):
     # the plane pass first, then the leading axes in place
-    assert len(_planes_of(kind, dims)) == 1
-    got, ref = _batch(kind, dims, 2, dev, seed=len(dims))
+    assert len(_planes_of(kind, dims, batch)) == 1
+    got, ref = _batch(kind, dims, batch, dev, seed=len(dims))
     assert O.rel_l2(got, ref) <= TOL, (kind, dims)
 
 
@@ -96,6 +98,7 @@ def test_per_axis_where_no_plane_fits():
     assert _planes_of("c", [256, 256, 256]) == []                 # 2^16-point planes
     assert _planes_of("c", [64, 16, 256]) == []                   # a side of 16
     assert _planes_of("c", [32, 32]) == []                        # 2^10 points
+    assert _planes_of("c", [128, 128], 255) == [] and _planes_of("c", [128, 128], 256) == [7]   # 2^14: >= 256
     assert [op.get("plane") for op in describe("c", [8, 64, 64], 1, G.afft_interleaved)["ops"]] == [0, 0, 0]
     assert [op.get("plane", 0) for op in describe("c", [8, 64, 64], 1, G.FORM_F64)["ops"]] == [0, 0, 0]
 

@@ -63,6 +63,38 @@ def test_tune_picks_the_fastest_and_plans_stay_correct(kind, dims, batch, dev):
     batched_parity(kind, dims, batch)
 
 
+def test_tune_weighs_plane_fusion(tmp_path, dev):
+    # the last two axes of a 3D transform: one plane-fused pass or one pass
+    # each; both timed, the faster kept
+    rep = G.tune("c", [16, 64, 64], 4)
+    cands = rep["candidates"]
+    assert {c["no_plane"] for c in cands} == {0, 1}, rep    # (2, fused at any count, is the rule here)
+    assert {c["launches"] for c in cands if c["no_plane"]} == {3} and {c["launches"] for c in cands
+                                                                      if not c["no_plane"]} == {2}, rep
+    timed = [c for c in cands if c["ms"] > 0]
+    assert rep["chosen"]["ms"] == min(c["ms"] for c in timed)
+    batched_parity("c", [16, 64, 64], 4)
+    # the per-axis form forced through the cache file, in a fresh process
+    name = torch.cuda.get_device_name(0).replace(" ", "_")
+    path = str(tmp_path / "tune_no_plane.json")
+    with open(path, "w") as f:
+        f.write("{\n\"%s|1|8x64x128|3|0\": {\"split\": 0, \"real_inv\": 0, \"cols_lsu\": 0, \"tc\": 0, "
+                "\"cols_c\": 0, \"passes\": 0, \"no_plane\": 1, \"ms\": 1.0}\n}\n" % name)
+    code = ("import sys; sys.path.insert(0, %r); sys.path.insert(0, %r)\n"
+            "import test_tune_gpu as T\nT.batched_parity('ci', [8, 64, 128], 3)\n" % (ROOT, os.path.join(ROOT, "tests")))
+    r = subprocess.run([sys.executable, "-c", code], env=dict(os.environ, AFFT_GB300_TUNE_CACHE=path),
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+
+
+def test_tune_weighs_large_planes_at_small_counts(dev):
+    # 2^14-point planes below 256 per launch: the rule takes a pass per
+    # axis, and the tuner also times the plane pass (no_plane = 2)
+    rep = G.tune("c", [8, 128, 128], 2)
+    assert {c["no_plane"] for c in rep["candidates"]} == {0, 2}, rep
+    batched_parity("c", [8, 128, 128], 2)
+
+
 def test_tune_shape_without_choices(dev):
     rep = G.tune("c", [1024], 64)
     assert len(rep["candidates"]) == 1 and rep["chosen"]["ms"] < 0
