@@ -89,8 +89,9 @@ bool get_cols_pipe(int logl, int kind, LineKernel* out);
 
 // plane-fused passes (plane_fft.cuh, k_plane*.cu): the last two axes of a
 // complex N-D transform, planes of 2^log1 rows x 2^log2 points with
-// 12 <= log1 + log2 <= 14 and both in [5, 9]
+// 8 <= log1 + log2 <= 14 and both in [4, 9]
 bool get_plane_kernel(int log1, int log2, LineKernel* out);
+bool get_plane_kernel_small(int log1, int log2, LineKernel* out);   // planes of at most 2^11 points
 
 // cols c2c passes (not transposing) with another tile width, for the
 // autotuner: 256 points in 8 or 32 lines, 512 points in 16; TMA-fed
@@ -179,7 +180,7 @@ LineKernel make_tma_kernel() {
   return k;
 }
 
-// a plane pass: one CTA per plane, D1 D2 / 16 threads
+// a plane pass: PPC planes per CTA, D1 D2 / 16 threads each
 template <int LOG1, int LOG2>
 LineKernel make_plane_kernel() {
   using PS = PlaneShape<LOG1, LOG2>;
@@ -195,7 +196,7 @@ LineKernel make_plane_kernel() {
   k.tstore = 0;
   k.tc = 0;
   k.unit = 1;
-  k.lines_per_cta = PS::D1;   // rows per plane: the grid is one CTA per plane
+  k.lines_per_cta = PS::PPC * PS::D1;   // rows per CTA: PPC planes of D1 rows
   k.threads = PS::NT;
   k.smem = (size_t)PS::FLOAT2S * sizeof(float2);
   k.halves = 1;

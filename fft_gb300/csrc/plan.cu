@@ -593,7 +593,8 @@ struct Builder {
     return get_plane_kernel(ilog2ll(d1), ilog2ll(d2), &k);
   }
 
-  // `count` dense planes of d1 rows x d2 points from A to B, one CTA each.
+  // `count` dense planes of d1 rows x d2 points from A to B (one or, for
+  // planes under 2^12 points, several per CTA).
   void plane(long long d1, long long d2, long long count, const View& A, const View& B, bool inverse) {
     if (!ok) return;
     Op op;
@@ -623,7 +624,8 @@ struct Builder {
         return;
       }
     }
-    op.grid = count;
+    const long long ppc = op.k.lines_per_cta / d1;   // planes per CTA
+    op.grid = (count + ppc - 1) / ppc;
     op.threads = op.k.threads;
     op.smem = op.k.smem;
     P.ops.push_back(op);

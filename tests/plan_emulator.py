@@ -133,14 +133,16 @@ def run_op(B, op):
     t = op["type"]
     if t == "line" and op.get("plane"):
         # plane-fused pass: plane q (D1 rows x D2 points, dense from its
-        # line offset) by one CTA, a 2D transform
+        # line offset), C / D1 planes per CTA, a 2D transform
         D1, D2 = 1 << op["plane"], 1 << op["logl"]
         n = op["nlines"] // D1
         q = np.arange(n, dtype=np.int64)
+        cta = q // (op["C"] // D1)
+        assert op["grid"] == -(-n // (op["C"] // D1))
         m = np.arange(D1 * D2)
-        x = _gather(B, acc, op["in"], q, m, q).reshape(n, D1, D2)
+        x = _gather(B, acc, op["in"], q, m, cta).reshape(n, D1, D2)
         y = np.fft.ifft2(x) * (D1 * D2) if op["inverse"] else np.fft.fft2(x)
-        pending += _scatter(B, acc, op["out"], q, m, q, y.reshape(n, D1 * D2))
+        pending += _scatter(B, acc, op["out"], q, m, cta, y.reshape(n, D1 * D2))
     elif t == "line":
         L = 1 << op["logl"]
         q = np.arange(op["nlines"], dtype=np.int64)

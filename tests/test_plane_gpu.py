@@ -16,7 +16,9 @@ torch = pytest.importorskip("torch")
 TOL = 2e-6
 
 # (log2 rows, log2 row length) of every plane_fft instantiation
-PLANES = [(5, 7), (6, 6), (7, 5), (5, 8), (6, 7), (7, 6), (8, 5), (5, 9), (6, 8), (7, 7), (8, 6), (9, 5)]
+PLANES = [(4, 4), (4, 5), (5, 4), (4, 6), (5, 5), (6, 4), (4, 7), (5, 6), (6, 5), (7, 4),
+          (4, 8), (5, 7), (6, 6), (7, 5), (8, 4), (4, 9), (5, 8), (6, 7), (7, 6), (8, 5), (9, 4),
+          (5, 9), (6, 8), (7, 7), (8, 6), (9, 5)]
 
 
 @pytest.fixture(scope="module")
@@ -58,7 +60,8 @@ def _planes_of(kind, dims, batch=1):
 def test_plane_2d(dev, kind, lg):
     dims = [1 << lg[0], 1 << lg[1]]
     # (2^14-point planes take the plane pass from 256 planes per launch)
-    batch = 256 if lg[0] + lg[1] == 14 else 3
+    # (planes under 2^12 points share a CTA: a batch that leaves the last CTA part full)
+    batch = 256 if lg[0] + lg[1] == 14 else 3 if lg[0] + lg[1] >= 12 else (1 << (12 - lg[0] - lg[1])) + 3
     assert _planes_of(kind, dims, batch) == [lg[0]]           # one plane pass is the whole transform
     for inplace in (False, True):
         got, ref = _batch(kind, dims, batch, dev, inplace=inplace, seed=lg[0] * 16 + lg[1])
@@ -67,7 +70,8 @@ def test_plane_2d(dev, kind, lg):
 
 @pytest.mark.parametrize("kind", ["c", "ci"])
 @pytest.mark.parametrize("dims,batch", [([8, 64, 64], 2), ([4, 32, 128], 2), ([16, 128, 128], 16), ([2, 256, 32], 2),
-                                        ([8, 32, 512], 32), ([2, 4, 64, 64], 2)], ids=str)
+                                        ([8, 32, 512], 32), ([2, 4, 64, 64], 2), ([16, 16, 16], 3),
+                                        ([4, 32, 32], 5), ([2, 16, 64], 7), ([64, 128, 16], 1)], ids=str)
 def test_plane_nd(dev, kind, dims, batch):
     # the plane pass first, then the leading axes in place
     assert len(_planes_of(kind, dims, batch)) == 1
@@ -78,13 +82,13 @@ def test_plane_nd(dev, kind, dims, batch):
 @pytest.mark.parametrize("pad", [1, 2])
 def test_plane_unaligned_loads(dev, pad):
     # planes that start off a 16-byte boundary load without the staging
-    for dims in ([64, 64], [32, 128], [8, 32, 256]):
+    for dims in ([64, 64], [32, 128], [8, 32, 256], [32, 32], [16, 16, 64]):
         got, ref = _batch("c", dims, 2, dev, pad=pad, seed=pad)
         assert O.rel_l2(got, ref) <= TOL, (dims, pad)
 
 
 @pytest.mark.parametrize("kind", ["r", "ri"])
-@pytest.mark.parametrize("dims", [[16, 64, 64], [8, 32, 128], [64, 128, 64]], ids=str)
+@pytest.mark.parametrize("dims", [[16, 64, 64], [8, 32, 128], [64, 128, 64], [16, 16, 16], [32, 32, 32]], ids=str)
 def test_plane_behind_real_pass(dev, kind, dims):
     from test_parity_gpu import check, inputs, run_plan
     assert len(_planes_of(kind, dims)) == 1
@@ -96,8 +100,9 @@ def test_per_axis_where_no_plane_fits():
     # planes of other sizes, sides below 32, the interleaved format and the
     # FP64 and tensor-core forms keep one pass per axis
     assert _planes_of("c", [256, 256, 256]) == []                 # 2^16-point planes
-    assert _planes_of("c", [64, 16, 256]) == []                   # a side of 16
-    assert _planes_of("c", [32, 32]) == []                        # 2^10 points
+    assert _planes_of("c", [64, 8, 256]) == []                    # a side of 8
+    assert _planes_of("c", [1024, 16]) == []                      # a side of 1024
+    assert _planes_of("c", [32, 32]) == [5]                       # 2^10 points: four planes per CTA
     assert _planes_of("c", [128, 128], 255) == [] and _planes_of("c", [128, 128], 256) == [7]   # 2^14: >= 256
     assert [op.get("plane") for op in describe("c", [8, 64, 64], 1, G.afft_interleaved)["ops"]] == [0, 0, 0]
     assert [op.get("plane", 0) for op in describe("c", [8, 64, 64], 1, G.FORM_F64)["ops"]] == [0, 0, 0]
