@@ -90,8 +90,13 @@ bool get_cols_pipe(int logl, int kind, LineKernel* out);
 // plane-fused passes (plane_fft.cuh, k_plane*.cu): the last two axes of a
 // complex N-D transform, planes of 2^log1 rows x 2^log2 points with
 // 8 <= log1 + log2 <= 14 and both in [4, 9]
-bool get_plane_kernel(int log1, int log2, LineKernel* out);
-bool get_plane_kernel_small(int log1, int log2, LineKernel* out);   // planes of at most 2^11 points
+// (unit 1 split planes, 2 interleaved pairs), by the per-unit, per-size
+// lookups of k_plane*.cu
+bool get_plane_kernel(int log1, int log2, int unit, LineKernel* out);
+bool get_plane_split_small(int log1, int log2, LineKernel* out);   // 2^8 .. 2^11 points
+bool get_plane_split_big(int log1, int log2, LineKernel* out);     // 2^12 .. 2^14 points
+bool get_plane_pairs_small(int log1, int log2, LineKernel* out);
+bool get_plane_pairs_big(int log1, int log2, LineKernel* out);
 
 // cols c2c passes (not transposing) with another tile width, for the
 // autotuner: 256 points in 8 or 32 lines, 512 points in 16; TMA-fed
@@ -181,12 +186,12 @@ LineKernel make_tma_kernel() {
 }
 
 // a plane pass: PPC planes per CTA, D1 D2 / 16 threads each
-template <int LOG1, int LOG2>
+template <int LOG1, int LOG2, int UNIT>
 LineKernel make_plane_kernel() {
   using PS = PlaneShape<LOG1, LOG2>;
   LineKernel k;
-  k.fn = &plane_fft<LOG1, LOG2>;
-  k.grouped = &plane_fft_grouped<LOG1, LOG2>;
+  k.fn = &plane_fft<LOG1, LOG2, UNIT>;
+  k.grouped = &plane_fft_grouped<LOG1, LOG2, UNIT>;
   k.tma = nullptr;
   k.grouped_tma = nullptr;
   k.logl = LOG2;
@@ -195,7 +200,7 @@ LineKernel make_plane_kernel() {
   k.kind = LK_C2C;
   k.tstore = 0;
   k.tc = 0;
-  k.unit = 1;
+  k.unit = UNIT;
   k.lines_per_cta = PS::PPC * PS::D1;   // rows per CTA: PPC planes of D1 rows
   k.threads = PS::NT;
   k.smem = (size_t)PS::FLOAT2S * sizeof(float2);

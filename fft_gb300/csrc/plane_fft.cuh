@@ -2,8 +2,8 @@
 // complex transform in one pass when a whole plane fits one CTA.
 //
 // A plane is D1 rows of D2 contiguous points (2^8 to 2^14 points, both sides
-// 16 to 512), planes dense one after another (split planes, unit element
-// stride).  A CTA transforms PPC = max(1, 2^12 / (D1 D2)) consecutive planes
+// 16 to 512), planes dense one after another: split planes at unit element
+// stride (UNIT 1) or interleaved re,im pairs (UNIT 2, 8-byte accesses).  A CTA transforms PPC = max(1, 2^12 / (D1 D2)) consecutive planes
 // with D1 D2 / 16 threads each (256 threads or more):
 //   - rows phase: the PPC D1 rows as rows-mode lines of D2 points (thread t
 //     of row r holds points t + T2 e), loaded as the rows kernels load them
@@ -56,8 +56,9 @@ struct PlaneShape {
 // p.nlines / D1 planes; p.in / p.out give plane q's base (line_off of q),
 // elements at unit stride, planes PPC apart contiguous (a multi-plane CTA
 // reads its planes as PPC D1 contiguous rows).
-template <int LOG1, int LOG2>
+template <int LOG1, int LOG2, int UNIT>
 __device__ __forceinline__ void plane_body(const LineParams& p, long long cta) {
+  static_assert(UNIT == 1 || UNIT == 2, "split planes or interleaved pairs");
   using PS = PlaneShape<LOG1, LOG2>;
   using S1 = Sched<LOG1>;
   using S2 = Sched<LOG2>;
@@ -80,16 +81,28 @@ __device__ __forceinline__ void plane_body(const LineParams& p, long long cta) {
       pr.in.re = p.in.re + bin;
       pr.in.im = p.in.im + bin;
       pr.nlines = (long long)here * D1;
-      rows_stage_in<LOG2, PPC * D1>(pr, 0, smr, v, t, r);
+      if constexpr (UNIT == 1) rows_stage_in<LOG2, PPC * D1>(pr, 0, smr, v, t, r);
+      else rows_stage_in_reals<LOG2, PPC * D1>(pr, 0, smr, v, t, r);   // pair lines: 2 D2 floats each
       staged = true;
     }
   }
   if (!staged) {
     if (r < here * D1) {
-      const float* pr = p.in.re + bin + r * D2 + t;
-      const float* pi = p.in.im + bin + r * D2 + t;
+      if constexpr (UNIT == 1) {
+        const float* pr = p.in.re + bin + r * D2 + t;
+        const float* pi = p.in.im + bin + r * D2 + t;
 #pragma unroll
-      for (int e = 0; e < E; e++) v[e] = make_float2(__ldg(pr + T2 * e), __ldg(pi + T2 * e));
+        for (int e = 0; e < E; e++) v[e] = make_float2(__ldg(pr + T2 * e), __ldg(pi + T2 * e));
+      } else {
+        const float* pz = p.in.re + bin + 2 * (r * D2 + t);
+        if (!(reinterpret_cast<uintptr_t>(pz) & 7)) {
+#pragma unroll
+          for (int e = 0; e < E; e++) v[e] = __ldg(reinterpret_cast<const float2*>(pz) + T2 * e);
+        } else {
+#pragma unroll
+          for (int e = 0; e < E; e++) v[e] = make_float2(__ldg(pz + 2 * T2 * e), __ldg(pz + 2 * T2 * e + 1));
+        }
+      }
     } else {
 #pragma unroll
       for (int e = 0; e < E; e++) v[e] = make_float2(0.f, 0.f);
@@ -125,24 +138,38 @@ __device__ __forceinline__ void plane_body(const LineParams& p, long long cta) {
       for (int e = 0; e < E; e++) v[e] = cswap(v[e]);
     }
     const long long bout = line_off(p.out, q0 + g);
-    float* pr = p.out.re + bout + t2 * D2 + c2;
-    float* pi = p.out.im + bout + t2 * D2 + c2;
+    if constexpr (UNIT == 1) {
+      float* pr = p.out.re + bout + t2 * D2 + c2;
+      float* pi = p.out.im + bout + t2 * D2 + c2;
 #pragma unroll
-    for (int e = 0; e < E; e++) {
-      pr[T1 * D2 * e] = v[e].x;
-      pi[T1 * D2 * e] = v[e].y;
+      for (int e = 0; e < E; e++) {
+        pr[T1 * D2 * e] = v[e].x;
+        pi[T1 * D2 * e] = v[e].y;
+      }
+    } else {
+      float* pz = p.out.re + bout + 2 * (t2 * D2 + c2);
+      if (!(reinterpret_cast<uintptr_t>(pz) & 7)) {
+#pragma unroll
+        for (int e = 0; e < E; e++) reinterpret_cast<float2*>(pz)[T1 * D2 * e] = v[e];
+      } else {
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+          pz[2 * T1 * D2 * e] = v[e].x;
+          pz[2 * T1 * D2 * e + 1] = v[e].y;
+        }
+      }
     }
   }
 }
 
-template <int LOG1, int LOG2>
+template <int LOG1, int LOG2, int UNIT>
 __global__ void __launch_bounds__(PlaneShape<LOG1, LOG2>::NT, min_ctas<PlaneShape<LOG1, LOG2>::NT>())
 plane_fft(const LineParams p) {
-  plane_body<LOG1, LOG2>(p, blockIdx.x);
+  plane_body<LOG1, LOG2, UNIT>(p, blockIdx.x);
 }
 
 // Its queue form (as line_fft_grouped): one CTA per virtual CTA.
-template <int LOG1, int LOG2>
+template <int LOG1, int LOG2, int UNIT>
 __global__ void __launch_bounds__(PlaneShape<LOG1, LOG2>::NT, min_ctas<PlaneShape<LOG1, LOG2>::NT>())
 plane_fft_grouped(const Segment* __restrict__ segs, const int* __restrict__ seg_of, long long total) {
   __shared__ LineParams sp;
@@ -151,7 +178,7 @@ plane_fft_grouped(const Segment* __restrict__ segs, const int* __restrict__ seg_
     __syncthreads();   // a previous iteration is done with sp and the buffer
     stage_params(sp, segs[sg].p);
     __syncthreads();
-    plane_body<LOG1, LOG2>(sp, v - segs[sg].cta0);
+    plane_body<LOG1, LOG2, UNIT>(sp, v - segs[sg].cta0);
   }
 }
 

@@ -79,6 +79,46 @@ def test_plane_nd(dev, kind, dims, batch):
     assert O.rel_l2(got, ref) <= TOL, (kind, dims)
 
 
+@pytest.mark.parametrize("dims,batch", [([64, 64], 3), ([32, 32], 7), ([8, 32, 128], 2), ([4, 16, 16], 5),
+                                        ([128, 128], 256)], ids=str)
+@pytest.mark.parametrize("kind", ["c", "ci"])
+@pytest.mark.parametrize("inplace", [False, True], ids=["oop", "inplace"])
+def test_plane_interleaved(dev, kind, dims, batch, inplace):
+    # interleaved re,im pairs: the pair kernels (staged 16-byte loads of pair
+    # lines, 8-byte stores)
+    from test_parity_gpu import run_batch
+    assert [op.get("plane") for op in describe(kind, dims, batch, G.afft_interleaved)["ops"]][0] == \
+        {64: 6, 32: 5, 16: 4, 128: 7}[dims[-2]]
+    n = int(np.prod(dims))
+    rng = np.random.default_rng(len(dims) + batch)
+    a = rng.uniform(-1, 1, n * batch).astype(np.float32)
+    b = rng.uniform(-1, 1, n * batch).astype(np.float32)
+    got = run_batch(kind, dims, batch, a, b, fmt=G.afft_interleaved, inplace=inplace)
+    outs = [O.oracle64(kind, dims, a[j * n:(j + 1) * n], b[j * n:(j + 1) * n]) for j in range(batch)]
+    ref = (np.concatenate([o[0] for o in outs]), np.concatenate([o[1] for o in outs]))
+    assert O.rel_l2(got, ref) <= TOL, (kind, dims, inplace)
+
+
+def test_plane_interleaved_unaligned(dev):
+    # interleaved planes off an 8- and a 16-byte boundary (scalar and unstaged pair accesses)
+    p = G.BatchPlan("c", [32, 64], 4, fmt=G.afft_interleaved)
+    n = 32 * 64 * 4
+    rng = np.random.default_rng(5)
+    a = rng.uniform(-1, 1, n).astype(np.float32)
+    b = rng.uniform(-1, 1, n).astype(np.float32)
+    src = np.empty(2 * n, np.float32)
+    src[0::2], src[1::2] = a, b
+    outs = [O.oracle64("c", [32, 64], a[j * 2048:(j + 1) * 2048], b[j * 2048:(j + 1) * 2048]) for j in range(4)]
+    ref = (np.concatenate([o[0] for o in outs]), np.concatenate([o[1] for o in outs]))
+    for pad in (1, 2):
+        s = _dev(src, dev, pad)
+        d = _dev(np.zeros_like(src), dev, pad)
+        p.launch(s, None, d, None)
+        torch.cuda.synchronize()
+        o = d.cpu().numpy()
+        assert O.rel_l2((o[0::2], o[1::2]), ref) <= TOL, pad
+
+
 @pytest.mark.parametrize("pad", [1, 2])
 def test_plane_unaligned_loads(dev, pad):
     # planes that start off a 16-byte boundary load without the staging
@@ -97,14 +137,13 @@ def test_plane_behind_real_pass(dev, kind, dims):
 
 
 def test_per_axis_where_no_plane_fits():
-    # planes of other sizes, sides below 32, the interleaved format and the
-    # FP64 and tensor-core forms keep one pass per axis
+    # planes of other sizes, sides below 16 or above 512, and the FP64 and
+    # tensor-core forms keep one pass per axis
     assert _planes_of("c", [256, 256, 256]) == []                 # 2^16-point planes
     assert _planes_of("c", [64, 8, 256]) == []                    # a side of 8
     assert _planes_of("c", [1024, 16]) == []                      # a side of 1024
     assert _planes_of("c", [32, 32]) == [5]                       # 2^10 points: four planes per CTA
     assert _planes_of("c", [128, 128], 255) == [] and _planes_of("c", [128, 128], 256) == [7]   # 2^14: >= 256
-    assert [op.get("plane") for op in describe("c", [8, 64, 64], 1, G.afft_interleaved)["ops"]] == [0, 0, 0]
     assert [op.get("plane", 0) for op in describe("c", [8, 64, 64], 1, G.FORM_F64)["ops"]] == [0, 0, 0]
 
 
