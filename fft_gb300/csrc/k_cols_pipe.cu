@@ -5,7 +5,9 @@ bool get_cols_pipe(int logl, int kind, LineKernel* out) {
   if (logl != 11) return false;
   switch (kind) {
     case LK_C2C: *out = make_pipe_kernel<11, LK_C2C>(); return true;
+#if AFFT_PIPE_R2C
     case LK_R2C: *out = make_pipe_kernel<11, LK_R2C>(); return true;
+#endif
     case LK_C2R: *out = make_pipe_kernel<11, LK_C2R>(); return true;
   }
   return false;

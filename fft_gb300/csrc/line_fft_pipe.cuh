@@ -38,6 +38,12 @@
 #ifndef AFFT_PIPE_BULK_STORE
 #define AFFT_PIPE_BULK_STORE 1
 #endif
+// the 2048-point R2C pass in this form too (unsplit, the post-pass mirrors
+// through the exchange buffer) instead of the split one-tile-per-two-CTAs
+// form: built and taken only when set (measured 20% slower)
+#ifndef AFFT_PIPE_R2C
+#define AFFT_PIPE_R2C 0
+#endif
 
 namespace agb {
 

@@ -395,11 +395,7 @@ static View inter_view(int b, long long off = 0) {  // re,im pairs in one array
 #ifndef AFFT_PLANE
 #define AFFT_PLANE 1
 #endif
-// the 2048-point R2C pass in that form too (unsplit), instead of the split
-// one-tile-per-two-CTAs form
-#ifndef AFFT_PIPE_R2C
-#define AFFT_PIPE_R2C 0
-#endif
+
 
 static IOSpec io(const View& v, long long es, long long lo, long long hi, int qshift, long long qmask) {
   IOSpec s;
