@@ -44,6 +44,11 @@
 #ifndef AFFT_PIPE_R2C
 #define AFFT_PIPE_R2C 0
 #endif
+// lines per tile: 8 (one 1024-thread CTA per SM, 200 KB) or 4 (two
+// 512-thread CTAs per SM, 100 KB each)
+#ifndef AFFT_PIPE_C
+#define AFFT_PIPE_C 8
+#endif
 
 namespace agb {
 
@@ -159,14 +164,14 @@ __device__ __forceinline__ void pipe_store_plane(const LineParams& p, const CUte
 // raw tile, bin L read directly).  Split planes in, split planes out; every
 // tile whole (the host's tma_tile rules).  ntiles = nlines / C.
 template <int LOGL, int C, int KIND>
-__global__ void __launch_bounds__(Sched<LOGL>::T * C, 1)
+__global__ void __launch_bounds__(Sched<LOGL>::T * C, 8 / C)
 line_fft_pipe(const LineParams p, const __grid_constant__ TmaTile tm, const __grid_constant__ TmaTile tmo,
               long long ntiles) {
   using Sc = Sched<LOGL>;
   constexpr int L = Sc::L, E = Sc::E, T = Sc::T;
   static_assert(KIND == LK_C2C || KIND == LK_R2C || KIND == LK_C2R, "plain cols kinds");
-  static_assert(LOGL == 11 && C == 8 && T == 128 && E == 16 && Sc::radix(0) == 8,
-                "the exchange rows are those of 8-line 2048-point tiles");
+  static_assert(LOGL == 11 && (C == 8 || C == 4) && T == 128 && E == 16 && Sc::radix(0) == 8,
+                "the exchange rows are those of 8- or 4-line 2048-point tiles");
   __shared__ __align__(8) uint64_t mbar;
   extern __shared__ __align__(1024) float2 smem_raw[];
   float* raw = reinterpret_cast<float*>(smem_raw);

@@ -1140,8 +1140,8 @@ int Plan::launch(const float* src_re, const float* src_im, float* dst_re, float*
       TmaTile tm, tmo{};
       if (op.k.pipe && sm_count > 0 && tma_tile(p, op.k, &tm) &&
           (!(AFFT_PIPE_BULK_STORE && op.k.kind == LK_C2C) || tma_tile_out(p, op.k, &tmo))) {
-        // persistent: at most one CTA per SM, each walking tiles gridDim.x apart
-        const long long g = std::min<long long>(op.grid, sm_count);
+        // persistent: at most pipe_ctas CTAs per SM, each walking tiles gridDim.x apart
+        const long long g = std::min<long long>(op.grid, (long long)sm_count * op.k.pipe_ctas);
         op.k.pipe<<<(unsigned)g, op.threads, op.k.pipe_smem, st>>>(p, tm, tmo, op.grid);
       } else if (op.k.tma && tma_tile(p, op.k, &tm)) {
         op.k.tma<<<(unsigned)op.grid, op.threads, op.smem, st>>>(p, tm);

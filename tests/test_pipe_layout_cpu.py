@@ -1,13 +1,14 @@
 """The exchange layout of the pipelined 2048-point cols kernels
 (fft_gb300/csrc/line_fft_pipe.cuh), restated: element j of line c at float
-(j + j/8) * 8 + c.  Checked here for every warp and element: the rows it
+(j + j/8) * C + c, for tiles of C = 8 and of C = 4 lines.  Checked here for every warp and element: the rows it
 gives are the Stockham positions of the stage scatter (stage() in
 line_fft.cuh) written as a per-thread base plus a compile-time offset, the
-map is injective and fits kPipeRows rows, and every access of a warp (4
-consecutive threads t x 8 lines) touches 32 distinct banks."""
+map is injective and fits kPipeRows rows, and every access of a warp (32/C
+consecutive threads t x C lines) touches 32 distinct banks."""
 import numpy as np
+import pytest
 
-L, C, T, E = 2048, 8, 128, 16
+L, T, E = 2048, 128, 16
 ROWS = L + L // 8                       # kPipeRows
 RADIX = [(8, 1), (16, 8)]               # (R, NS) of the two stages that scatter
 
@@ -47,25 +48,31 @@ def test_every_position_is_written_once_per_stage():
         assert pos == list(range(L))
 
 
-def test_injective_and_in_bounds():
+@pytest.mark.parametrize("C", [8, 4])
+def test_injective_and_in_bounds(C):
     idx = np.array([row(j) * C + c for j in range(L) for c in range(C)])
     assert len(set(idx.tolist())) == L * C and idx.max() < ROWS * C
 
 
-def test_one_wavefront_per_access():
+@pytest.mark.parametrize("C", [8, 4])
+def test_one_wavefront_per_access(C):
+    # a warp covers 32 / C consecutive threads t (lanes C apart share a line)
+    W = 32 // C
     for w in range(T * C // 32):
-        ts = [4 * w + k for k in range(4)]
+        ts = [W * w + k for k in range(W)]
         for e in range(E):
             for f in (lambda t: grow(t, e), lambda t: wrow(0, t, e), lambda t: wrow(1, t, e)):
                 banks = {(f(t) * C + c) % 32 for t in ts for c in range(C)}
                 assert len(banks) == 32, (w, e)
 
 
-def test_raw_tile_reads_one_wavefront():
-    # the raw tile is [rows][C] per plane; the C2R pre-pass also reads the
-    # mirror rows L - i
+@pytest.mark.parametrize("C", [8, 4])
+def test_raw_tile_reads_one_wavefront(C):
+    # the raw tile is [rows][C] per plane (as is the bulk stores' staging);
+    # the C2R pre-pass also reads the mirror rows L - i
+    W = 32 // C
     for w in range(T * C // 32):
-        ts = [4 * w + k for k in range(4)]
+        ts = [W * w + k for k in range(W)]
         for e in range(E):
             for f in (lambda t: t + T * e, lambda t: (L - (t + T * e)) % L):
                 banks = {(f(t) * C + c) % 32 for t in ts for c in range(C)}
