@@ -1,0 +1,91 @@
+"""GPU parity of the persistent TMA-pipelined 2048-point cols passes
+(line_fft_pipe: C2C with TMA output stores, C2R) against the FP64 oracle:
+tile counts below, at and above one per SM and not multiples of the grid,
+in place and out of place, the four-step twiddle, and arrays off a 16-byte
+boundary, where the one-tile-per-CTA kernels of the same shape run instead.
+Tolerance: relative L2 <= 2e-6, as the other parity tests."""
+import numpy as np
+import pytest
+
+import fft_gb300 as G
+from oracle import oracle as O
+from plan_emulator import describe
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+TOL = 2e-6
+
+
+@pytest.fixture(scope="module")
+def dev():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch.device("cuda:0")
+
+
+def _pipe_ops(kind, dims, batch):
+    return [op for op in describe(kind, dims, batch)["ops"] if op["type"] == "line" and op.get("pipe")]
+
+
+def _c2c(kind, dims, batch, dev, pad=0, inplace=False, seed=0):
+    from test_plane_gpu import _batch
+    got, ref = _batch(kind, dims, batch, dev, inplace=inplace, pad=pad, seed=seed)
+    return O.rel_l2(got, ref)
+
+
+# tiles of 8 columns (one per transform of 8 columns): 1 tile, 151 / 152 /
+# 153 tiles around one per SM, 2048 tiles (13.5 per SM)
+@pytest.mark.parametrize("dims,batch", [([2048, 8], 1), ([2048, 8], 151), ([2048, 8], 152), ([2048, 8], 153),
+                                        ([2048, 2048], 8), ([4, 2048, 64], 3)], ids=str)
+@pytest.mark.parametrize("kind", ["c", "ci"])
+def test_pipe_c2c_tile_counts(dev, kind, dims, batch):
+    assert len(_pipe_ops(kind, dims, batch)) == 1
+    for inplace in (False, True):
+        err = _c2c(kind, dims, batch, dev, inplace=inplace, seed=dims[-1])
+        assert err <= TOL, (kind, dims, batch, inplace, err)
+
+
+@pytest.mark.parametrize("pad", [1, 2])
+def test_pipe_c2c_unaligned_takes_the_one_tile_kernels(dev, pad):
+    # the same plans on arrays off a 16-byte boundary: tma_tile refuses the
+    # maps and the LSU kernel of the same shape runs
+    for dims, batch in (([2048, 64], 2), ([2048, 2048], 1)):
+        assert _c2c("c", dims, batch, dev, pad=pad, seed=pad) <= TOL, (dims, pad)
+
+
+@pytest.mark.parametrize("kind,dims", [("c", [1 << 21, 8]), ("ci", [1 << 21, 4]), ("c", [1 << 22, 2])], ids=str)
+def test_pipe_c2c_fourstep_twiddle(dev, kind, dims):
+    # strided axes of 2^21 and 2^22 points: pass A of their four-step is a
+    # 2048-point pipelined cols pass that applies the four-step twiddle
+    ops = _pipe_ops(kind, dims, 1)
+    assert ops and ops[0]["tw_n"] == dims[0], ops
+    assert _c2c(kind, dims, 1, dev, seed=3) <= TOL, (kind, dims)
+
+
+@pytest.mark.parametrize("dims,batch", [([4096, 8], 1), ([4096, 8], 153), ([4096, 4096], 2), ([4096, 64, 16], 3)],
+                         ids=str)
+def test_pipe_c2r_tile_counts(dev, dims, batch):
+    # the real inverse's dim-0 pass (2048 complex points) pipelined
+    from test_parity_gpu import check, inputs
+    assert len(_pipe_ops("ri", dims, batch)) == 1
+    n = int(np.prod(dims))
+    h = O.half_elems(dims)
+    rng = np.random.default_rng(batch)
+    a = rng.standard_normal(h * batch).astype(np.float32)
+    b = rng.standard_normal(h * batch).astype(np.float32)
+    p = G.BatchPlan("ri", dims, batch)
+    sr, si = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
+    d = torch.zeros(n * batch, dtype=torch.float32, device=dev)
+    p.launch(sr, si, d, None)
+    torch.cuda.synchronize()
+    got = d.cpu().numpy()
+    for j in range(batch):
+        ref = O.oracle64("ri", dims, a[j * h:(j + 1) * h], b[j * h:(j + 1) * h])
+        assert O.rel_l2(got[j * n:(j + 1) * n], ref) <= TOL, (dims, batch, j)
+
+
+def test_pipe_c2r_unaligned(dev):
+    from test_parity_gpu import check, inputs, run_plan
+    for pad in (1, 3):
+        a, b = inputs("ri", [4096, 64], pad)
+        check("ri", [4096, 64], a, b, run_plan("ri", [4096, 64], a, b, dev, pad=pad))
