@@ -1441,50 +1441,61 @@ __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map
       : "memory");
 }
 
-// Loads the tile of CTA `cta` into dst ([re rows][C] then [im rows][C]
-// floats).  Every thread waits, bounded; on a timeout the error word is set,
-// the copies get a second bounded wait, and the whole CTA returns false.
+// Thread 0's part of a tile load: (re)initialise the barrier at mb and issue
+// the tile of CTA `cta` into dst ([re rows][C] then [im rows][C] floats, or
+// [rows][2 C] for pairs).  The coordinates need only the input's column mask
+// and shift.  Other threads may wait on the barrier only after a CTA barrier
+// that follows this call.
 template <int C>
-__device__ __forceinline__ bool tma_load_tile(const LineParams& p, const TmaTile& tm, long long cta, uint64_t* mbar,
-                                              void* dst) {
-  const uint32_t mb = smem_u32(mbar);
+__device__ __forceinline__ void tma_issue_tile(long long qmask, int qshift, const TmaTile& tm, long long cta,
+                                               uint32_t mb, void* dst) {
   const long long q0 = cta * C;
-  const int col = (int)(q0 & p.in.qmask);
-  const int outer = (int)(q0 >> p.in.qshift);
-  if (threadIdx.x == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb));
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    const uint32_t bytes = 2u * (uint32_t)tm.rows * C * 4u;
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(bytes) : "memory");
-    const uint32_t d = smem_u32(dst);
-    if (tm.pairs) {
-      // one array of pairs: the tile is [rows][2 C floats], column col at float 2 col
-      for (int r = 0; r < tm.rows; r += tm.box_rows)
-        tma_load_3d(d + (uint32_t)r * C * 8u, &tm.re, 2 * col, r, outer, mb);
-    } else {
-      const uint32_t plane = (uint32_t)tm.rows * C * 4u;
-      for (int r = 0; r < tm.rows; r += tm.box_rows) {
-        tma_load_3d(d + (uint32_t)r * C * 4u, &tm.re, col, r, outer, mb);
-        tma_load_3d(d + plane + (uint32_t)r * C * 4u, &tm.im, col, r, outer, mb);
-      }
+  const int col = (int)(q0 & qmask);
+  const int outer = (int)(q0 >> qshift);
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb));
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  const int rows = tm.rows, br = tm.box_rows;
+  const uint32_t bytes = 2u * (uint32_t)rows * C * 4u;
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(bytes) : "memory");
+  const uint32_t d = smem_u32(dst);
+  if (tm.pairs) {
+    // one array of pairs: the tile is [rows][2 C floats], column col at float 2 col
+    for (int r = 0; r < rows; r += br) tma_load_3d(d + (uint32_t)r * C * 8u, &tm.re, 2 * col, r, outer, mb);
+  } else {
+    const uint32_t plane = (uint32_t)rows * C * 4u;
+    for (int r = 0; r < rows; r += br) {
+      tma_load_3d(d + (uint32_t)r * C * 4u, &tm.re, col, r, outer, mb);
+      tma_load_3d(d + plane + (uint32_t)r * C * 4u, &tm.im, col, r, outer, mb);
     }
   }
+}
+
+// Every thread waits for the tile, bounded; on success thread 0 invalidates
+// the barrier (a later tile of the same CTA sets it up again); on a timeout
+// the error word is set, the copies get a second bounded wait, and the whole
+// CTA returns false.
+__device__ __forceinline__ bool tma_wait_tile(uint32_t mb, int* err) {
   const bool ok = __syncthreads_and(tc_wait(mb, 0));
-  // every thread has passed the wait: the barrier may be set up again by a
-  // later tile of the same CTA (grouped launches)
   if (ok && threadIdx.x == 0) asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(mb) : "memory");
   if (!ok) {
     if (threadIdx.x == 0) {
-      if (p.err) atomicExch(p.err, 2);
+      if (err) atomicExch(err, 2);
       tc_wait(mb, 0);   // let copies still in flight land before the CTA's shared memory goes away
     }
     __syncthreads();
   }
   return ok;
+}
+
+// Loads the tile of CTA `cta` into dst (as tma_issue_tile) and waits for it.
+template <int C>
+__device__ __forceinline__ bool tma_load_tile(const LineParams& p, const TmaTile& tm, long long cta, uint64_t* mbar,
+                                              void* dst) {
+  const uint32_t mb = smem_u32(mbar);
+  if (threadIdx.x == 0) tma_issue_tile<C>(p.in.qmask, p.in.qshift, tm, cta, mb, dst);
+  __syncthreads();   // the barrier's set-up is visible before anyone waits on it
+  return tma_wait_tile(mb, p.err);
 }
 
 template <int LOGL, int C, int KIND, bool TSTORE = false, int UNIT = 0>
@@ -1528,13 +1539,21 @@ line_fft_grouped(const Segment* __restrict__ segs, const int* __restrict__ seg_o
     static_assert(COLS && !TC, "TMA tiles: cols passes");
     __shared__ __align__(8) uint64_t mbar;
     extern __shared__ __align__(1024) float2 smem_raw[];
+    const uint32_t mb = smem_u32(&mbar);
     for (long long v = blockIdx.x; v < total; v += gridDim.x) {
       const int sg = __ldg(seg_of + v);
-      __syncthreads();
+      const long long cta = v - __ldg(&segs[sg].cta0);
+      __syncthreads();   // the previous virtual CTA is done with sp, the barrier and the buffer
+      // the tile's loads go out before the parameters are staged, straight
+      // from the segment's column mask, shift and tensor maps (the mixed
+      // queue 12.52 -> 12.45 ms against loading after the staging)
+      if (threadIdx.x == 0)
+        tma_issue_tile<C>(__ldg(&segs[sg].p.in.qmask), __ldg(&segs[sg].p.in.qshift), *segs[sg].tma, cta, mb,
+                          smem_raw);
       stage_params(sp, segs[sg].p);
-      __syncthreads();
-      if (!tma_load_tile<C>(sp, *segs[sg].tma, v - segs[sg].cta0, &mbar, smem_raw)) return;
-      line_fft_body<LOGL, C, true, KIND, TSTORE, false, UNIT, true>(sp, v - segs[sg].cta0);
+      __syncthreads();   // parameters staged, the barrier's set-up visible
+      if (!tma_wait_tile(mb, sp.err)) return;
+      line_fft_body<LOGL, C, true, KIND, TSTORE, false, UNIT, true>(sp, cta);
     }
     return;
   }
