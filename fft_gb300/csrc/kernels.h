@@ -34,6 +34,7 @@ struct LineKernel {
                                      // launched on at most one CTA per SM with the tile count
   size_t pipe_smem = 0;              // its dynamic shared memory (raw tile + exchange buffer)
   int pipe_ctas = 1;                 // its resident CTAs per SM (the grid is at most that many per SM)
+  GroupedKernelFn grouped_pipe = nullptr;   // its queue form (segments with tensor maps), or null
   int plane_log1 = 0;                // plane kernels (plane_fft): log2 of the rows per plane (the column
                                      // axis); logl is then log2 of the row length; 0 for line kernels
 };
@@ -216,6 +217,7 @@ LineKernel make_pipe_kernel() {
   constexpr int C = AFFT_PIPE_C;
   LineKernel k = make_tma_kernel<LOGL, KIND, C>();
   k.pipe = &line_fft_pipe<LOGL, C, KIND>;
+  k.grouped_pipe = &line_fft_pipe_grouped<LOGL, C, KIND>;
   static_assert(LOGL == 11, "the pipelined kernels are built for 2048-point lines");
   k.pipe_smem = ((size_t)2 * (1 << LOGL) + kPipeRows) * C * sizeof(float);   // raw tile + exchange rows
   k.pipe_ctas = 8 / C;

@@ -103,7 +103,7 @@ __device__ __forceinline__ void pipe_exchange(float2 (&v)[Sched<LOGL>::E], int t
 
 // All stages of one tile, values in registers in the canonical layout on
 // entry and exit (as run_stages).
-template <int LOGL, int C, int KIND, int S, class Hook>
+template <int LOGL, int C, int KIND, bool BULK, int S, class Hook>
 __device__ __forceinline__ void pipe_stages(float2 (&v)[Sched<LOGL>::E], int t, int c, const float2* tw,
                                             float* xs, const Hook& hook) {
   using Sc = Sched<LOGL>;
@@ -113,13 +113,13 @@ __device__ __forceinline__ void pipe_stages(float2 (&v)[Sched<LOGL>::E], int t, 
     stage<R, NS, Sc::E, Sc::T, true, false, 0, packed_bfly<LOGL, true>()>(v, t, c, tw + Sc::twoff(S), xs, false,
                                                                          nullptr);
     if constexpr (S + 1 < Sc::NSTAGES) {
-      constexpr bool TRAIL = S + 2 < Sc::NSTAGES || KIND == LK_R2C || pipe_bulk<KIND>();
+      constexpr bool TRAIL = S + 2 < Sc::NSTAGES || KIND == LK_R2C || BULK;
       if constexpr (S == 0) {
         pipe_exchange<LOGL, C, S, TRAIL>(v, t, c, xs, hook);
       } else {
         pipe_exchange<LOGL, C, S, TRAIL>(v, t, c, xs, [] {});
       }
-      pipe_stages<LOGL, C, KIND, S + 1>(v, t, c, tw, xs, hook);
+      pipe_stages<LOGL, C, KIND, BULK, S + 1>(v, t, c, tw, xs, hook);
     }
   }
 }
@@ -127,11 +127,11 @@ __device__ __forceinline__ void pipe_stages(float2 (&v)[Sched<LOGL>::E], int t, 
 // Issue the TMA loads of tile `tile` (C adjacent columns of one outer block,
 // both planes, boxes of C columns x box_rows rows) on the barrier at mb.
 template <int L, int C>
-__device__ __forceinline__ void pipe_issue(const LineParams& p, const TmaTile& tm, long long tile, uint32_t raw,
-                                           uint32_t mb) {
+__device__ __forceinline__ void pipe_issue(long long qmask, int qshift, const TmaTile& tm, long long tile,
+                                           uint32_t raw, uint32_t mb) {
   const long long q0 = tile * C;
-  const int col = (int)(q0 & p.in.qmask);
-  const int outer = (int)(q0 >> p.in.qshift);
+  const int col = (int)(q0 & qmask);
+  const int outer = (int)(q0 >> qshift);
   constexpr uint32_t plane = (uint32_t)L * C * 4u;
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(2u * plane) : "memory");
   for (int r = 0; r < L; r += tm.box_rows) {
@@ -159,28 +159,28 @@ __device__ __forceinline__ void pipe_store_plane(const LineParams& p, const CUte
   asm volatile("cp.async.bulk.commit_group;" ::: "memory");
 }
 
+// The tile loop of the pipelined kernels.  This CTA takes tiles first,
+// first + gridDim.x, ... < ntiles; prep(v, &cta) returns the parameters of
+// tile v (and its CTA index within them), and issue(v) (thread 0) issues
+// tile v's loads on the barrier at mb.  The grouped form's prep stages the
+// parameters in shared memory, behind a CTA barrier of its own.
+//
 // KIND: LK_C2C (with the four-step twiddle when p.tw_n), LK_R2C (unsplit:
 // the post-pass through the exchange buffer), LK_C2R (the pre-pass from the
 // raw tile, bin L read directly).  Split planes in, split planes out; every
-// tile whole (the host's tma_tile rules).  ntiles = nlines / C.
-template <int LOGL, int C, int KIND>
-__global__ void __launch_bounds__(Sched<LOGL>::T * C, 8 / C)
-line_fft_pipe(const LineParams p, const __grid_constant__ TmaTile tm, const __grid_constant__ TmaTile tmo,
-              long long ntiles) {
+// tile whole (the host's tma_tile rules).  BULK: the output planes go out by
+// TMA (the output maps tmo; C2C only).
+template <int LOGL, int C, int KIND, bool BULK, class Prep, class Issue>
+__device__ __forceinline__ void pipe_loop(long long first, long long ntiles, uint32_t mb, float* raw, float* xs,
+                                          const TmaTile* tmo, const Prep& prep, const Issue& issue) {
   using Sc = Sched<LOGL>;
   constexpr int L = Sc::L, E = Sc::E, T = Sc::T;
   static_assert(KIND == LK_C2C || KIND == LK_R2C || KIND == LK_C2R, "plain cols kinds");
   static_assert(LOGL == 11 && (C == 8 || C == 4) && T == 128 && E == 16 && Sc::radix(0) == 8,
                 "the exchange rows are those of 8- or 4-line 2048-point tiles");
-  __shared__ __align__(8) uint64_t mbar;
-  extern __shared__ __align__(1024) float2 smem_raw[];
-  float* raw = reinterpret_cast<float*>(smem_raw);
-  float* xs = raw + 2 * L * C;
+  static_assert(!BULK || KIND == LK_C2C, "TMA stores: the complex pass");
   const int tid = threadIdx.x;
   const int c = tid % C, t = tid / C;
-  const uint32_t mb = smem_u32(&mbar);
-  const uint32_t raw_s = smem_u32(raw);
-  constexpr bool BULK = pipe_bulk<KIND>();
 
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb));
@@ -188,13 +188,15 @@ line_fft_pipe(const LineParams p, const __grid_constant__ TmaTile tm, const __gr
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
   __syncthreads();
-  if (tid == 0 && (long long)blockIdx.x < ntiles) pipe_issue<L, C>(p, tm, blockIdx.x, raw_s, mb);
+  if (tid == 0 && first < ntiles) issue(first);
 
   uint32_t phase = 0;
-  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, phase ^= 1u) {
+  for (long long tile = first; tile < ntiles; tile += gridDim.x, phase ^= 1u) {
     // the previous tile's bulk stores have read the exchange buffer before
     // anyone writes it again
     if (BULK && tid == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+    long long cta;
+    const LineParams& p = prep(tile, &cta);
     if (!__syncthreads_and(tc_wait(mb, phase))) {
       if (tid == 0) {
         if (p.err) atomicExch(p.err, 2);
@@ -203,7 +205,7 @@ line_fft_pipe(const LineParams p, const __grid_constant__ TmaTile tm, const __gr
       __syncthreads();
       return;
     }
-    const long long q = tile * C + c;
+    const long long q = cta * C + c;
     float2 v[E];
     if constexpr (KIND == LK_C2R) {
       // real inverse pre-pass (onedim.hpp:1064-1068 / multi.hpp:366-370 with
@@ -247,15 +249,15 @@ line_fft_pipe(const LineParams p, const __grid_constant__ TmaTile tm, const __gr
     auto issue_next = [&] {
       if (tid == 0 && tile + gridDim.x < ntiles) {
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        pipe_issue<L, C>(p, tm, tile + gridDim.x, raw_s, mb);
+        issue(tile + gridDim.x);
       }
     };
     if constexpr (AFFT_PIPE_LATE_ISSUE) {
-      pipe_stages<LOGL, C, KIND, 0>(v, t, c, p.tw, xs, issue_next);
+      pipe_stages<LOGL, C, KIND, BULK, 0>(v, t, c, p.tw, xs, issue_next);
     } else {
       __syncthreads();
       issue_next();
-      pipe_stages<LOGL, C, KIND, 0>(v, t, c, p.tw, xs, [] {});
+      pipe_stages<LOGL, C, KIND, BULK, 0>(v, t, c, p.tw, xs, [] {});
     }
 
     const long long base = line_off(p.out, q);
@@ -288,7 +290,7 @@ line_fft_pipe(const LineParams p, const __grid_constant__ TmaTile tm, const __gr
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       __syncthreads();
       if (tid == 0) {
-        pipe_store_plane<L, C>(p, &tmo.re, tmo.box_rows, tile, xs_s);
+        pipe_store_plane<L, C>(p, &tmo->re, tmo->box_rows, cta, xs_s);
         asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
       }
       __syncthreads();
@@ -296,7 +298,7 @@ line_fft_pipe(const LineParams p, const __grid_constant__ TmaTile tm, const __gr
       for (int e = 0; e < E; e++) st[e * T * C] = v[e].y;
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       __syncthreads();
-      if (tid == 0) pipe_store_plane<L, C>(p, &tmo.im, tmo.box_rows, tile, xs_s);
+      if (tid == 0) pipe_store_plane<L, C>(p, &tmo->im, tmo->box_rows, cta, xs_s);
     } else if constexpr (KIND == LK_C2C || KIND == LK_C2R) {
 #pragma unroll
       for (int e = 0; e < E; e++) {
@@ -342,6 +344,53 @@ line_fft_pipe(const LineParams p, const __grid_constant__ TmaTile tm, const __gr
   }
   // the last tile's bulk stores have read shared memory before the CTA ends
   if (BULK && tid == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+
+// One plan launch: tiles 0 .. ntiles - 1 of the parameters p, their input
+// maps tm (and output maps tmo for the TMA stores).
+template <int LOGL, int C, int KIND>
+__global__ void __launch_bounds__(Sched<LOGL>::T * C, 8 / C)
+line_fft_pipe(const __grid_constant__ LineParams p, const __grid_constant__ TmaTile tm,
+              const __grid_constant__ TmaTile tmo, long long ntiles) {
+  __shared__ __align__(8) uint64_t mbar;
+  extern __shared__ __align__(1024) float2 smem_raw[];
+  float* raw = reinterpret_cast<float*>(smem_raw);
+  const uint32_t mb = smem_u32(&mbar), raw_s = smem_u32(raw);
+  pipe_loop<LOGL, C, KIND, pipe_bulk<KIND>()>(
+      blockIdx.x, ntiles, mb, raw, raw + 2 * Sched<LOGL>::L * C, &tmo,
+      [&](long long tile, long long* cta) -> const LineParams& {
+        *cta = tile;
+        return p;
+      },
+      [&](long long tile) { pipe_issue<Sched<LOGL>::L, C>(p.in.qmask, p.in.qshift, tm, tile, raw_s, mb); });
+}
+
+// The queue form: the group's virtual tiles (segments of several transforms,
+// every one with tensor maps), one persistent CTA per SM walking them; each
+// tile's loads go out from its segment's column mask, shift and maps, and
+// its parameters are staged in shared memory when its turn comes.
+template <int LOGL, int C, int KIND>
+__global__ void __launch_bounds__(Sched<LOGL>::T * C, 8 / C)
+line_fft_pipe_grouped(const Segment* __restrict__ segs, const int* __restrict__ seg_of, long long total) {
+  __shared__ LineParams sp;
+  __shared__ __align__(8) uint64_t mbar;
+  extern __shared__ __align__(1024) float2 smem_raw[];
+  float* raw = reinterpret_cast<float*>(smem_raw);
+  const uint32_t mb = smem_u32(&mbar), raw_s = smem_u32(raw);
+  pipe_loop<LOGL, C, KIND, false>(
+      blockIdx.x, total, mb, raw, raw + 2 * Sched<LOGL>::L * C, nullptr,
+      [&](long long v, long long* cta) -> const LineParams& {
+        const int sg = __ldg(seg_of + v);
+        *cta = v - __ldg(&segs[sg].cta0);
+        __syncthreads();   // the previous tile is done with sp
+        stage_params(sp, segs[sg].p);   // visible after the tile wait's barrier
+        return sp;
+      },
+      [&](long long v) {
+        const int sg = __ldg(seg_of + v);
+        pipe_issue<Sched<LOGL>::L, C>(__ldg(&segs[sg].p.in.qmask), __ldg(&segs[sg].p.in.qshift), *segs[sg].tma,
+                                      v - __ldg(&segs[sg].cta0), raw_s, mb);
+      });
 }
 
 }  // namespace agb

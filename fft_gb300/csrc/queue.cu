@@ -35,6 +35,7 @@ struct Group {
   std::vector<int> preds;  // groups this one waits for (sorted indices)
   bool line = true;
   LineKernel k{};
+  bool pipe = false;     // the persistent pipelined kernel (grid at most pipe_ctas per SM)
   std::vector<Segment> segs;
   std::vector<EwSegment> esegs;
   long long total = 0;   // virtual CTAs / blocks
@@ -92,6 +93,12 @@ static int build_queue(QueueImpl& Q) {
   std::vector<std::shared_ptr<Plan>> plan_of;
   std::vector<long long> scr_off;
   long long arena_floats = 0;
+  int dev = 0, sm_count = 0;   // SMs of the device: the pipelined groups' grid bound (0: none of those)
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    cudaGetLastError();
+    sm_count = 0;
+  }
   for (const auto& d : Q.descs) {
     int nd;
     long long dims[64];
@@ -111,10 +118,9 @@ static int build_queue(QueueImpl& Q) {
     auto it = Q.plans.find(key);
     if (it == Q.plans.end()) {
       // the tuned choice (for queues created with it), else what a plan of
-      // this shape gets; grouped launches have no pipelined form
+      // this shape gets
       Tuning tq = Q.tuned ? tuned_for_queue(d.kind, nd, dims)
                           : (Q.form == 0 ? tuned_choice(d.kind, nd, dims, 1, 0) : Tuning{});
-      tq.no_pipe = 1;
       if (tq.no_plane == 0) tq.no_plane = 2;   // one grouped launch gathers the planes of every transform
       auto P = build_plan(d.kind, nd, dims, 1, 0, false, Q.form, &tq);
       if (!P) return AFFT_GB300_EINVAL;
@@ -145,10 +151,14 @@ static int build_queue(QueueImpl& Q) {
       }
       // a TMA-capable pass whose tensor maps encode for this transform's
       // arrays goes to the TMA form of the grouped kernel
+      // (the pipelined 2048-point passes: their persistent queue form)
       TmaTile tm;
       const bool tma = op.type == OP_LINE && op.k.grouped_tma && tma_tile(bind_line_params(op, base), op.k, &tm);
+      const bool pipe = tma && op.k.grouped_pipe && sm_count > 0;
       const void* kid = op.type != OP_LINE ? (const void*)&elementwise_grouped
-                                           : (tma ? (const void*)op.k.grouped_tma : (const void*)op.k.grouped);
+                        : pipe            ? (const void*)op.k.grouped_pipe
+                        : tma             ? (const void*)op.k.grouped_tma
+                                          : (const void*)op.k.grouped;
       auto key = std::make_pair((int)i, kid);
       auto it = gidx.find(key);
       if (it == gidx.end()) {
@@ -157,7 +167,8 @@ static int build_queue(QueueImpl& Q) {
         g.id = (int)Q.groups.size();
         g.line = op.type == OP_LINE;
         g.k = op.k;
-        if (tma) g.k.grouped = op.k.grouped_tma;
+        if (tma) g.k.grouped = pipe ? op.k.grouped_pipe : op.k.grouped_tma;
+        g.pipe = pipe;
         it = gidx.emplace(key, Q.groups.size()).first;
         Q.groups.push_back(g);
       }
@@ -223,7 +234,7 @@ static int build_queue(QueueImpl& Q) {
       host = g.segs.data();
       bytes = g.segs.size() * sizeof(Segment);
       g.threads = g.k.threads;
-      g.smem = g.k.smem;
+      g.smem = g.pipe ? g.k.pipe_smem : g.k.smem;
       if (g.smem > 48 * 1024 &&
           cudaFuncSetAttribute((const void*)g.k.grouped, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)g.smem) != cudaSuccess) {
@@ -231,7 +242,7 @@ static int build_queue(QueueImpl& Q) {
         set_error(AFFT_GB300_ECUDA, "kernel shared memory configuration failed");
         return AFFT_GB300_ECUDA;
       }
-      g.grid = (int)g.total;
+      g.grid = (int)(g.pipe ? std::min<long long>(g.total, (long long)sm_count * g.k.pipe_ctas) : g.total);
     } else {
       std::stable_sort(g.esegs.begin(), g.esegs.end(),
                        [](const EwSegment& a, const EwSegment& b) { return a.blk0 > b.blk0; });
