@@ -576,14 +576,15 @@ struct Builder {
 
   // Whether the last two axes (d1 rows of d2 points) of a complex N-D
   // transform from A to B take one plane-fused pass: both views split or
-  // both interleaved pairs, the shapes plane_fft is built for, FP32 plain
-  // form, not tuned off.
+  // both interleaved pairs, the shapes plane_fft is built for, FP32 (the
+  // plane pass is plain FP32 in the tensor-core form too, as every pass
+  // without a tensor-core kernel), not tuned off.
   // A 2^14-point plane fills an SM with one CTA, so below 256 planes per
   // launch the per-axis passes keep more of the GPU busy (32 planes of
   // 128 x 128: 0.0184 vs 0.0198 ms) unless the plane is asked for (the
   // queue, whose grouped launches gather the planes of many transforms).
   bool plane_fits(long long d1, long long d2, long long count, const View& A, const View& B) const {
-    if (!AFFT_PLANE || f64 || P.form == FORM_TC || tune.no_plane == 1 || A.unit != B.unit || A.unit > 2) return false;
+    if (!AFFT_PLANE || f64 || tune.no_plane == 1 || A.unit != B.unit || A.unit > 2) return false;
     if (d1 < 2 || d2 < 2 || (d1 & (d1 - 1)) || (d2 & (d2 - 1))) return false;
     if (tune.no_plane == 0 && d1 * d2 >= (1LL << 14) && count < 256) return false;
     LineKernel k;

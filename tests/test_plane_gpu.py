@@ -137,14 +137,15 @@ def test_plane_behind_real_pass(dev, kind, dims):
 
 
 def test_per_axis_where_no_plane_fits():
-    # planes of other sizes, sides below 16 or above 512, and the FP64 and
-    # tensor-core forms keep one pass per axis
+    # planes of other sizes, sides below 16 or above 512, and the FP64 form
+    # keep one pass per axis (the tensor-core form takes the plain plane pass)
     assert _planes_of("c", [256, 256, 256]) == []                 # 2^16-point planes
     assert _planes_of("c", [64, 8, 256]) == []                    # a side of 8
     assert _planes_of("c", [1024, 16]) == []                      # a side of 1024
     assert _planes_of("c", [32, 32]) == [5]                       # 2^10 points: four planes per CTA
     assert _planes_of("c", [128, 128], 255) == [] and _planes_of("c", [128, 128], 256) == [7]   # 2^14: >= 256
     assert [op.get("plane", 0) for op in describe("c", [8, 64, 64], 1, G.FORM_F64)["ops"]] == [0, 0, 0]
+    assert [op.get("plane", 0) for op in describe("c", [8, 64, 64], 1, G.FORM_TC)["ops"]] == [6, 0]
 
 
 def test_queue_with_plane_segments(dev):
