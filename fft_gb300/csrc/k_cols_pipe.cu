@@ -1,7 +1,16 @@
-// 2048-point cols passes in the persistent TMA-pipelined form (line_fft_pipe)
+// 1024- and 2048-point cols passes in the persistent TMA-pipelined form (line_fft_pipe)
 #include "kernels.h"
 namespace agb {
 bool get_cols_pipe(int logl, int kind, LineKernel* out) {
+#if AFFT_PIPE10
+  if (logl == 10) {
+    switch (kind) {
+      case LK_C2C: *out = make_pipe_kernel<10, LK_C2C>(); return true;
+      case LK_C2R: *out = make_pipe_kernel<10, LK_C2R>(); return true;
+    }
+    return false;
+  }
+#endif
   if (logl != 11) return false;
   switch (kind) {
     case LK_C2C: *out = make_pipe_kernel<11, LK_C2C>(); return true;

@@ -214,13 +214,13 @@ LineKernel make_plane_kernel() {
 // a 2048-point cols pass with its pipelined form (AFFT_PIPE_C lines per tile)
 template <int LOGL, int KIND>
 LineKernel make_pipe_kernel() {
-  constexpr int C = AFFT_PIPE_C;
+  constexpr int C = LOGL == 11 ? AFFT_PIPE_C : 8;
   LineKernel k = make_tma_kernel<LOGL, KIND, C>();
   k.pipe = &line_fft_pipe<LOGL, C, KIND>;
   k.grouped_pipe = &line_fft_pipe_grouped<LOGL, C, KIND>;
-  static_assert(LOGL == 11, "the pipelined kernels are built for 2048-point lines");
-  k.pipe_smem = ((size_t)2 * (1 << LOGL) + kPipeRows) * C * sizeof(float);   // raw tile + exchange rows
-  k.pipe_ctas = 8 / C;
+  static_assert(LOGL == 11 || LOGL == 10, "the pipelined kernels are built for 1024- and 2048-point lines");
+  k.pipe_smem = ((size_t)2 * (1 << LOGL) + pipe_rows<LOGL>()) * C * sizeof(float);   // raw tile + exchange rows
+  k.pipe_ctas = 1024 / (Sched<LOGL>::T * C);
   return k;
 }
 

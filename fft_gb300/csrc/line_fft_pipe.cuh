@@ -49,6 +49,11 @@
 #ifndef AFFT_PIPE_C
 #define AFFT_PIPE_C 8
 #endif
+// the 1024-point complex and C2R cols passes in this form too (8-line tiles,
+// two 512-thread CTAs per SM, 104 KB each)
+#ifndef AFFT_PIPE10
+#define AFFT_PIPE10 1
+#endif
 
 namespace agb {
 
@@ -58,23 +63,40 @@ constexpr bool pipe_bulk() {
   return AFFT_PIPE_BULK_STORE && KIND == LK_C2C;
 }
 
-// Rows of the exchange buffer for the 2048-point schedule (radix 8, 16, 16;
-// T = 128, E = 16).  Stage 0 scatters output e = u + 2 r of butterfly
-// b = t + 128 u to element 8 b + r, stage 1 output e of butterfly t to element
-// 128 (t / 8) + t % 8 + 8 e, and the gather takes element t + 128 e; with
-// row = j + j/8 these are base(t) + offset(e).
-constexpr int kPipeRows = 2048 + 2048 / 8;
-template <int S>
+// Rows of the exchange buffer.  2048-point schedule (radix 8, 16, 16; T =
+// 128): row = j + j/8.  Stage 0 scatters output e = u + 2 r of butterfly
+// b = t + 128 u to element 8 b + r, stage 1 output e of butterfly t to
+// element 128 (t / 8) + t % 8 + 8 e, and the gather takes element t + 128 e.
+// 1024-point schedule (radix 4, 16, 16; T = 64): row = j + j/4.  Stage 0
+// scatters output e = u + 4 r of butterfly b = t + 64 u to element 4 b + r,
+// stage 1 output e of butterfly t to element 64 (t / 4) + t % 4 + 4 e, the
+// gather takes element t + 64 e.  Each is base(t) + offset(e).
+template <int LOGL>
+__host__ __device__ constexpr int pipe_rows() {
+  return LOGL == 11 ? 2048 + 2048 / 8 : 1024 + 1024 / 4;
+}
+template <int LOGL>
+__device__ __forceinline__ int pipe_row(int j) {
+  return LOGL == 11 ? j + (j >> 3) : j + (j >> 2);
+}
+template <int LOGL, int S>
 __device__ __forceinline__ int pipe_wbase(int t) {
-  return S == 0 ? 9 * t : 144 * (t >> 3) + (t & 7);
+  if constexpr (LOGL == 11) return S == 0 ? 9 * t : 144 * (t >> 3) + (t & 7);
+  else return S == 0 ? 5 * t : 80 * (t >> 2) + (t & 3);
 }
-template <int S>
+template <int LOGL, int S>
 __host__ __device__ constexpr int pipe_woff(int e) {
-  return S == 0 ? 1152 * (e % 2) + e / 2 : 9 * e;
+  if constexpr (LOGL == 11) return S == 0 ? 1152 * (e % 2) + e / 2 : 9 * e;
+  else return S == 0 ? 320 * (e % 4) + e / 4 : 5 * e;
 }
-__device__ __forceinline__ int pipe_gbase(int t) { return t + (t >> 3); }
-__host__ __device__ constexpr int pipe_goff(int e) { return 144 * e; }
-__device__ __forceinline__ int pipe_row(int j) { return j + (j >> 3); }
+template <int LOGL>
+__device__ __forceinline__ int pipe_gbase(int t) {
+  return LOGL == 11 ? t + (t >> 3) : t + (t >> 2);
+}
+template <int LOGL>
+__host__ __device__ constexpr int pipe_goff(int e) {
+  return LOGL == 11 ? 144 * e : 80 * e;
+}
 
 // The exchange after stage S: every value to its stage-S position, then
 // element t + T e of this thread's line back, re parts first, then im parts.
@@ -83,21 +105,21 @@ __device__ __forceinline__ int pipe_row(int j) { return j + (j >> 3); }
 template <int LOGL, int C, int S, bool TRAIL, class Hook>
 __device__ __forceinline__ void pipe_exchange(float2 (&v)[Sched<LOGL>::E], int t, int c, float* xs, const Hook& hook) {
   constexpr int E = Sched<LOGL>::E;
-  float* w = xs + pipe_wbase<S>(t) * C + c;
-  const float* g = xs + pipe_gbase(t) * C + c;
+  float* w = xs + pipe_wbase<LOGL, S>(t) * C + c;
+  const float* g = xs + pipe_gbase<LOGL>(t) * C + c;
   float nx[E];
 #pragma unroll
-  for (int e = 0; e < E; e++) w[pipe_woff<S>(e) * C] = v[e].x;
+  for (int e = 0; e < E; e++) w[pipe_woff<LOGL, S>(e) * C] = v[e].x;
   __syncthreads();
   hook();
 #pragma unroll
-  for (int e = 0; e < E; e++) nx[e] = g[pipe_goff(e) * C];
+  for (int e = 0; e < E; e++) nx[e] = g[pipe_goff<LOGL>(e) * C];
   __syncthreads();
 #pragma unroll
-  for (int e = 0; e < E; e++) w[pipe_woff<S>(e) * C] = v[e].y;
+  for (int e = 0; e < E; e++) w[pipe_woff<LOGL, S>(e) * C] = v[e].y;
   __syncthreads();
 #pragma unroll
-  for (int e = 0; e < E; e++) v[e] = make_float2(nx[e], g[pipe_goff(e) * C]);
+  for (int e = 0; e < E; e++) v[e] = make_float2(nx[e], g[pipe_goff<LOGL>(e) * C]);
   if constexpr (TRAIL) __syncthreads();
 }
 
@@ -176,8 +198,9 @@ __device__ __forceinline__ void pipe_loop(long long first, long long ntiles, uin
   using Sc = Sched<LOGL>;
   constexpr int L = Sc::L, E = Sc::E, T = Sc::T;
   static_assert(KIND == LK_C2C || KIND == LK_R2C || KIND == LK_C2R, "plain cols kinds");
-  static_assert(LOGL == 11 && (C == 8 || C == 4) && T == 128 && E == 16 && Sc::radix(0) == 8,
-                "the exchange rows are those of 8- or 4-line 2048-point tiles");
+  static_assert(((LOGL == 11 && (C == 8 || C == 4) && Sc::radix(0) == 8) || (LOGL == 10 && C == 8 && Sc::radix(0) == 4)) &&
+                    E == 16,
+                "the exchange rows are those of 8- or 4-line 2048-point and 8-line 1024-point tiles");
   static_assert(!BULK || KIND == LK_C2C, "TMA stores: the complex pass");
   const int tid = threadIdx.x;
   const int c = tid % C, t = tid / C;
@@ -312,19 +335,19 @@ __device__ __forceinline__ void pipe_loop(long long first, long long ntiles, uin
       // Z[L-k] comes through the exchange buffer, re parts then im parts.
       float mx[E];
 #pragma unroll
-      for (int e = 0; e < E; e++) xs[(pipe_gbase(t) + pipe_goff(e)) * C + c] = v[e].x;
+      for (int e = 0; e < E; e++) xs[(pipe_gbase<LOGL>(t) + pipe_goff<LOGL>(e)) * C + c] = v[e].x;
       __syncthreads();
 #pragma unroll
-      for (int e = 0; e < E; e++) mx[e] = xs[pipe_row((L - (t + T * e)) & (L - 1)) * C + c];
+      for (int e = 0; e < E; e++) mx[e] = xs[pipe_row<LOGL>((L - (t + T * e)) & (L - 1)) * C + c];
       __syncthreads();
 #pragma unroll
-      for (int e = 0; e < E; e++) xs[(pipe_gbase(t) + pipe_goff(e)) * C + c] = v[e].y;
+      for (int e = 0; e < E; e++) xs[(pipe_gbase<LOGL>(t) + pipe_goff<LOGL>(e)) * C + c] = v[e].y;
       __syncthreads();
 #pragma unroll
       for (int e = 0; e < E; e++) {
         const int k = t + T * e;
         const float2 s0 = v[e];
-        const float2 s1 = make_float2(mx[e], xs[pipe_row((L - k) & (L - 1)) * C + c]);
+        const float2 s1 = make_float2(mx[e], xs[pipe_row<LOGL>((L - k) & (L - 1)) * C + c]);
         float2 x;
         if (k == 0) {
           x = make_float2(s0.x + s0.y, 0.f);
@@ -349,7 +372,7 @@ __device__ __forceinline__ void pipe_loop(long long first, long long ntiles, uin
 // One plan launch: tiles 0 .. ntiles - 1 of the parameters p, their input
 // maps tm (and output maps tmo for the TMA stores).
 template <int LOGL, int C, int KIND>
-__global__ void __launch_bounds__(Sched<LOGL>::T * C, 8 / C)
+__global__ void __launch_bounds__(Sched<LOGL>::T * C, 1024 / (Sched<LOGL>::T * C))
 line_fft_pipe(const __grid_constant__ LineParams p, const __grid_constant__ TmaTile tm,
               const __grid_constant__ TmaTile tmo, long long ntiles) {
   __shared__ __align__(8) uint64_t mbar;
@@ -370,7 +393,7 @@ line_fft_pipe(const __grid_constant__ LineParams p, const __grid_constant__ TmaT
 // tile's loads go out from its segment's column mask, shift and maps, and
 // its parameters are staged in shared memory when its turn comes.
 template <int LOGL, int C, int KIND>
-__global__ void __launch_bounds__(Sched<LOGL>::T * C, 8 / C)
+__global__ void __launch_bounds__(Sched<LOGL>::T * C, 1024 / (Sched<LOGL>::T * C))
 line_fft_pipe_grouped(const Segment* __restrict__ segs, const int* __restrict__ seg_of, long long total) {
   __shared__ LineParams sp;
   __shared__ __align__(8) uint64_t mbar;

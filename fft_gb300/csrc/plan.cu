@@ -1139,10 +1139,14 @@ int Plan::launch(const float* src_re, const float* src_im, float* dst_re, float*
       p.in = bind(op.in, base, esz);
       p.out = bind(op.out, base, esz);
       TmaTile tm, tmo{};
-      if (op.k.pipe && sm_count > 0 && tma_tile(p, op.k, &tm) &&
+      // (1024-point tiles take the pipelined kernel from two per CTA slot:
+      // with one each it has nothing to prefetch and its float exchange
+      // costs more, 2048² c2r 0.0324 vs 0.0300 ms)
+      const long long slots = (long long)sm_count * op.k.pipe_ctas;
+      if (op.k.pipe && sm_count > 0 && (op.k.logl == 11 || op.grid >= 2 * slots) && tma_tile(p, op.k, &tm) &&
           (!(AFFT_PIPE_BULK_STORE && op.k.kind == LK_C2C) || tma_tile_out(p, op.k, &tmo))) {
         // persistent: at most pipe_ctas CTAs per SM, each walking tiles gridDim.x apart
-        const long long g = std::min<long long>(op.grid, (long long)sm_count * op.k.pipe_ctas);
+        const long long g = std::min<long long>(op.grid, slots);
         op.k.pipe<<<(unsigned)g, op.threads, op.k.pipe_smem, st>>>(p, tm, tmo, op.grid);
       } else if (op.k.tma && tma_tile(p, op.k, &tm)) {
         op.k.tma<<<(unsigned)op.grid, op.threads, op.smem, st>>>(p, tm);

@@ -154,7 +154,10 @@ static int build_queue(QueueImpl& Q) {
       // (the pipelined 2048-point passes: their persistent queue form)
       TmaTile tm;
       const bool tma = op.type == OP_LINE && op.k.grouped_tma && tma_tile(bind_line_params(op, base), op.k, &tm);
-      const bool pipe = tma && op.k.grouped_pipe && sm_count > 0;
+      // (2048-point passes only: the 1024-point ones measured 0.7% slower on
+      // the mixed queue than their one-tile grouped form, whose CTAs share
+      // the SMs with the groups running beside them)
+      const bool pipe = tma && op.k.grouped_pipe && sm_count > 0 && op.k.logl == 11;
       const void* kid = op.type != OP_LINE ? (const void*)&elementwise_grouped
                         : pipe            ? (const void*)op.k.grouped_pipe
                         : tma             ? (const void*)op.k.grouped_tma

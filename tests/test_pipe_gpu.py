@@ -1,5 +1,6 @@
-"""GPU parity of the persistent TMA-pipelined 2048-point cols passes
-(line_fft_pipe: C2C with TMA output stores, C2R) against the FP64 oracle:
+"""GPU parity of the persistent TMA-pipelined 1024- and 2048-point cols
+passes (line_fft_pipe: C2C, with TMA output stores at 2048 points, and C2R)
+against the FP64 oracle:
 tile counts below, at and above one per SM and not multiples of the grid,
 in place and out of place, the four-step twiddle, and arrays off a 16-byte
 boundary, where the one-tile-per-CTA kernels of the same shape run instead.
@@ -89,3 +90,31 @@ def test_pipe_c2r_unaligned(dev):
     for pad in (1, 3):
         a, b = inputs("ri", [4096, 64], pad)
         check("ri", [4096, 64], a, b, run_plan("ri", [4096, 64], a, b, dev, pad=pad))
+
+
+# 1024-point tiles: the pipelined kernel from two tiles per CTA slot (608 on
+# 152 SMs), the one-tile kernels below that; both sides of the threshold
+@pytest.mark.parametrize("kind,dims,batch", [("c", [1024, 8], 1216), ("ci", [1024, 8], 700), ("c", [1024, 1024], 4),
+                                             ("ci", [2, 1024, 512], 3)], ids=str)
+def test_pipe_1024_c2c(dev, kind, dims, batch):
+    assert len(_pipe_ops(kind, dims, batch)) == 1
+    for inplace in (False, True):
+        assert _c2c(kind, dims, batch, dev, inplace=inplace, seed=batch) <= TOL, (kind, dims, batch, inplace)
+
+
+@pytest.mark.parametrize("dims,batch", [([2048, 8], 700), ([2048, 2048], 4), ([2048, 2048], 1)], ids=str)
+def test_pipe_1024_c2r(dev, dims, batch):
+    assert len(_pipe_ops("ri", dims, batch)) == 1
+    n = int(np.prod(dims))
+    h = O.half_elems(dims)
+    rng = np.random.default_rng(batch + 1)
+    a = rng.standard_normal(h * batch).astype(np.float32)
+    b = rng.standard_normal(h * batch).astype(np.float32)
+    p = G.BatchPlan("ri", dims, batch)
+    d = torch.zeros(n * batch, dtype=torch.float32, device=dev)
+    p.launch(torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda(), d, None)
+    torch.cuda.synchronize()
+    got = d.cpu().numpy()
+    for j in range(batch):
+        ref = O.oracle64("ri", dims, a[j * h:(j + 1) * h], b[j * h:(j + 1) * h])
+        assert O.rel_l2(got[j * n:(j + 1) * n], ref) <= TOL, (dims, batch, j)

@@ -202,7 +202,8 @@ def test_long_real_scratch_is_pairs():
 @pytest.mark.parametrize("kind,dims,batch,expect", [
     ("c", [256, 256, 256], 1, [(0, 0), (1, 0), (1, 0)]),   # rows, then two 256-point cols passes by TMA
     ("c", [65536], 64, [(1, 0), (1, 0)]),                  # four-step: pass A (transposing store) and pass B by TMA
-    ("c", [1024, 1024], 4, [(0, 0), (1, 0)]),              # 1024-point cols pass by TMA
+    ("c", [1024, 1024], 4, [(0, 0), (1, 1)]),              # 1024-point cols pass pipelined (taken at launch
+                                                           # from two tiles per CTA slot)
     ("ri", [4096, 4096], 1, [(0, 0), (1, 1)]),             # the 2048-point C2R pass pipelined
     ("r", [4096, 4096], 1, [(0, 0), (0, 0)]),              # the split 2048-point R2C pass keeps LSU loads (measured)
     ("c", [2048, 2048], 2, [(0, 0), (1, 1)]),              # the 2048-point C2C cols pass pipelined
@@ -210,8 +211,8 @@ def test_long_real_scratch_is_pairs():
 ], ids=str)
 def test_tma_fed_passes(kind, dims, batch, expect):
     """Which passes take the TMA-fed cols kernels, as (tma, pipe): the plan's
-    default choice.  pipe: the persistent pipelined form of the 2048-point
-    cols passes.  At launch the LSU kernel of the same shape runs instead
+    default choice.  pipe: the persistent pipelined form of the 1024- and
+    2048-point cols passes.  At launch the LSU kernel of the same shape runs instead
     where the bound arrays miss the TMA alignment rules."""
     d = describe(kind, dims, batch)
     got = [(op.get("tma", 0), op.get("pipe", 0)) for op in d["ops"] if op["type"] == "line"]
