@@ -21,4 +21,13 @@ bool get_cols_pipe(int logl, int kind, LineKernel* out) {
   }
   return false;
 }
+bool get_cols_pipe_tstore(int logl, LineKernel* out) {
+#if AFFT_PIPE10_TSTORE
+  if (logl == 10) {
+    *out = make_pipe_kernel<10, LK_C2C, true>();
+    return true;
+  }
+#endif
+  return false;
+}
 }  // namespace agb

@@ -88,6 +88,8 @@ bool get_cols_tma_pairs(int logl, bool tstore, int pairs, LineKernel* out);
 // persistent TMA-pipelined form (k_cols_pipe.cu): out->pipe set, out->tma and
 // out->fn the one-tile-per-CTA kernels of the same shape
 bool get_cols_pipe(int logl, int kind, LineKernel* out);
+// the 1024-point four-step pass A (transposing store, split planes) in that form
+bool get_cols_pipe_tstore(int logl, LineKernel* out);
 
 // plane-fused passes (plane_fft.cuh, k_plane*.cu): the last two axes of a
 // complex N-D transform, planes of 2^log1 rows x 2^log2 points with
@@ -212,12 +214,12 @@ LineKernel make_plane_kernel() {
 }
 
 // a 2048-point cols pass with its pipelined form (AFFT_PIPE_C lines per tile)
-template <int LOGL, int KIND>
+template <int LOGL, int KIND, bool TSTORE = false>
 LineKernel make_pipe_kernel() {
   constexpr int C = LOGL == 11 ? AFFT_PIPE_C : 8;
-  LineKernel k = make_tma_kernel<LOGL, KIND, C>();
-  k.pipe = &line_fft_pipe<LOGL, C, KIND>;
-  k.grouped_pipe = &line_fft_pipe_grouped<LOGL, C, KIND>;
+  LineKernel k = make_tma_kernel<LOGL, KIND, C, TSTORE>();
+  k.pipe = &line_fft_pipe<LOGL, C, KIND, TSTORE>;
+  k.grouped_pipe = TSTORE ? nullptr : &line_fft_pipe_grouped<LOGL, C, KIND>;
   static_assert(LOGL == 11 || LOGL == 10, "the pipelined kernels are built for 1024- and 2048-point lines");
   k.pipe_smem = ((size_t)2 * (1 << LOGL) + pipe_rows<LOGL>()) * C * sizeof(float);   // raw tile + exchange rows
   k.pipe_ctas = 1024 / (Sched<LOGL>::T * C);

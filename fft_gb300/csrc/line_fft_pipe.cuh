@@ -54,6 +54,12 @@
 #ifndef AFFT_PIPE10
 #define AFFT_PIPE10 1
 #endif
+// and the 1024-point four-step pass A (transposing store): built and taken
+// only when set (measured 2-4% slower than the one-tile TMA kernel at large
+// batches: 2^20 x 64 c2c 0.4717 vs 0.4553 ms)
+#ifndef AFFT_PIPE10_TSTORE
+#define AFFT_PIPE10_TSTORE 0
+#endif
 
 namespace agb {
 
@@ -98,6 +104,12 @@ __host__ __device__ constexpr int pipe_goff(int e) {
   return LOGL == 11 ? 144 * e : 80 * e;
 }
 
+// The transposing store's staging of 8-line 1024-point tiles: element k of
+// line c at k * 8 + ((c + k / 4) & 7).  Written in the cols mapping (4
+// consecutive k x 8 lines per warp) and read along lines (32 consecutive k of
+// one line per warp), both on 32 distinct banks.
+__device__ __forceinline__ int pipe_tsidx(int k, int c) { return k * 8 + ((c + (k >> 2)) & 7); }
+
 // The exchange after stage S: every value to its stage-S position, then
 // element t + T e of this thread's line back, re parts first, then im parts.
 // TRAIL: the buffer is written again before the next CTA-wide barrier.
@@ -125,7 +137,9 @@ __device__ __forceinline__ void pipe_exchange(float2 (&v)[Sched<LOGL>::E], int t
 
 // All stages of one tile, values in registers in the canonical layout on
 // entry and exit (as run_stages).
-template <int LOGL, int C, int KIND, bool BULK, int S, class Hook>
+// XOUT: the exchange buffer is written again after the stages (TMA stores,
+// the transposing store), so the last exchange ends with a barrier.
+template <int LOGL, int C, int KIND, bool XOUT, int S, class Hook>
 __device__ __forceinline__ void pipe_stages(float2 (&v)[Sched<LOGL>::E], int t, int c, const float2* tw,
                                             float* xs, const Hook& hook) {
   using Sc = Sched<LOGL>;
@@ -135,13 +149,13 @@ __device__ __forceinline__ void pipe_stages(float2 (&v)[Sched<LOGL>::E], int t, 
     stage<R, NS, Sc::E, Sc::T, true, false, 0, packed_bfly<LOGL, true>()>(v, t, c, tw + Sc::twoff(S), xs, false,
                                                                          nullptr);
     if constexpr (S + 1 < Sc::NSTAGES) {
-      constexpr bool TRAIL = S + 2 < Sc::NSTAGES || KIND == LK_R2C || BULK;
+      constexpr bool TRAIL = S + 2 < Sc::NSTAGES || KIND == LK_R2C || XOUT;
       if constexpr (S == 0) {
         pipe_exchange<LOGL, C, S, TRAIL>(v, t, c, xs, hook);
       } else {
         pipe_exchange<LOGL, C, S, TRAIL>(v, t, c, xs, [] {});
       }
-      pipe_stages<LOGL, C, KIND, BULK, S + 1>(v, t, c, tw, xs, hook);
+      pipe_stages<LOGL, C, KIND, XOUT, S + 1>(v, t, c, tw, xs, hook);
     }
   }
 }
@@ -192,7 +206,7 @@ __device__ __forceinline__ void pipe_store_plane(const LineParams& p, const CUte
 // raw tile, bin L read directly).  Split planes in, split planes out; every
 // tile whole (the host's tma_tile rules).  BULK: the output planes go out by
 // TMA (the output maps tmo; C2C only).
-template <int LOGL, int C, int KIND, bool BULK, class Prep, class Issue>
+template <int LOGL, int C, int KIND, bool BULK, bool TSTORE, class Prep, class Issue>
 __device__ __forceinline__ void pipe_loop(long long first, long long ntiles, uint32_t mb, float* raw, float* xs,
                                           const TmaTile* tmo, const Prep& prep, const Issue& issue) {
   using Sc = Sched<LOGL>;
@@ -202,6 +216,8 @@ __device__ __forceinline__ void pipe_loop(long long first, long long ntiles, uin
                     E == 16,
                 "the exchange rows are those of 8- or 4-line 2048-point and 8-line 1024-point tiles");
   static_assert(!BULK || KIND == LK_C2C, "TMA stores: the complex pass");
+  static_assert(!TSTORE || (KIND == LK_C2C && LOGL == 10 && C == 8 && !BULK),
+                "the transposing store: 8-line 1024-point complex tiles");
   const int tid = threadIdx.x;
   const int c = tid % C, t = tid / C;
 
@@ -276,17 +292,57 @@ __device__ __forceinline__ void pipe_loop(long long first, long long ntiles, uin
       }
     };
     if constexpr (AFFT_PIPE_LATE_ISSUE) {
-      pipe_stages<LOGL, C, KIND, BULK, 0>(v, t, c, p.tw, xs, issue_next);
+      pipe_stages<LOGL, C, KIND, BULK || TSTORE, 0>(v, t, c, p.tw, xs, issue_next);
     } else {
       __syncthreads();
       issue_next();
-      pipe_stages<LOGL, C, KIND, BULK, 0>(v, t, c, p.tw, xs, [] {});
+      pipe_stages<LOGL, C, KIND, BULK || TSTORE, 0>(v, t, c, p.tw, xs, [] {});
     }
 
     const long long base = line_off(p.out, q);
     const long long S = (long long)T * p.out.es;
     float* pr = p.out.re + base + (long long)t * p.out.es;
     float* pi = p.out.im + base + (long long)t * p.out.es;
+    if constexpr (TSTORE) {
+      // four-step pass A: computed across lines, stored along them with the
+      // four-step twiddle (as line_fft_body's transposing store), re parts
+      // then im parts through the staging layout
+      const int c2 = tid / T, t2 = tid % T;
+      const long long q2 = cta * C + c2;
+      float rx[E];
+#pragma unroll
+      for (int e = 0; e < E; e++) xs[pipe_tsidx(t + T * e, c)] = v[e].x;
+      __syncthreads();
+#pragma unroll
+      for (int e = 0; e < E; e++) rx[e] = xs[pipe_tsidx(t2 + T * e, c2)];
+      __syncthreads();
+#pragma unroll
+      for (int e = 0; e < E; e++) xs[pipe_tsidx(t + T * e, c)] = v[e].y;
+      __syncthreads();
+#pragma unroll
+      for (int e = 0; e < E; e++) v[e] = make_float2(rx[e], xs[pipe_tsidx(t2 + T * e, c2)]);
+      if (p.tw_n && p.tw_full) {
+#pragma unroll
+        for (int e = 0; e < E; e++) v[e] = cmul(v[e], fourstep_twiddle<L, true>(p, q2, t2 + T * e));
+      } else if (p.tw_n) {
+#pragma unroll
+        for (int e = 0; e < E; e++) v[e] = cmul(v[e], fourstep_twiddle<L, false>(p, q2, t2 + T * e));
+      }
+      if (p.inverse) {
+#pragma unroll
+        for (int e = 0; e < E; e++) v[e] = cswap(v[e]);
+      }
+      const long long b2 = line_off(p.out, q2);
+      const long long S2 = (long long)T * p.out.es;
+      float* r2 = p.out.re + b2 + (long long)t2 * p.out.es;
+      float* i2 = p.out.im + b2 + (long long)t2 * p.out.es;
+#pragma unroll
+      for (int e = 0; e < E; e++) {
+        r2[e * S2] = v[e].x;
+        i2[e * S2] = v[e].y;
+      }
+      continue;   // the next tile's first write to the buffer follows its own barriers
+    }
     if constexpr (KIND == LK_C2C) {
       if (p.tw_n && p.tw_full) {
 #pragma unroll
@@ -371,7 +427,7 @@ __device__ __forceinline__ void pipe_loop(long long first, long long ntiles, uin
 
 // One plan launch: tiles 0 .. ntiles - 1 of the parameters p, their input
 // maps tm (and output maps tmo for the TMA stores).
-template <int LOGL, int C, int KIND>
+template <int LOGL, int C, int KIND, bool TSTORE = false>
 __global__ void __launch_bounds__(Sched<LOGL>::T * C, 1024 / (Sched<LOGL>::T * C))
 line_fft_pipe(const __grid_constant__ LineParams p, const __grid_constant__ TmaTile tm,
               const __grid_constant__ TmaTile tmo, long long ntiles) {
@@ -379,7 +435,7 @@ line_fft_pipe(const __grid_constant__ LineParams p, const __grid_constant__ TmaT
   extern __shared__ __align__(1024) float2 smem_raw[];
   float* raw = reinterpret_cast<float*>(smem_raw);
   const uint32_t mb = smem_u32(&mbar), raw_s = smem_u32(raw);
-  pipe_loop<LOGL, C, KIND, pipe_bulk<KIND>()>(
+  pipe_loop<LOGL, C, KIND, pipe_bulk<KIND>() && !TSTORE, TSTORE>(
       blockIdx.x, ntiles, mb, raw, raw + 2 * Sched<LOGL>::L * C, &tmo,
       [&](long long tile, long long* cta) -> const LineParams& {
         *cta = tile;
@@ -400,7 +456,7 @@ line_fft_pipe_grouped(const Segment* __restrict__ segs, const int* __restrict__ 
   extern __shared__ __align__(1024) float2 smem_raw[];
   float* raw = reinterpret_cast<float*>(smem_raw);
   const uint32_t mb = smem_u32(&mbar), raw_s = smem_u32(raw);
-  pipe_loop<LOGL, C, KIND, false>(
+  pipe_loop<LOGL, C, KIND, false, false>(
       blockIdx.x, total, mb, raw, raw + 2 * Sched<LOGL>::L * C, nullptr,
       [&](long long v, long long* cta) -> const LineParams& {
         const int sg = __ldg(seg_of + v);

@@ -502,9 +502,11 @@ struct Builder {
     // unsplit); at launch the one-tile-per-CTA kernels of the same shape run
     // where the bound arrays miss the TMA rules
     LineKernel kp;
-    if (AFFT_COLS_PIPE && !f64 && !tc && cols && !tstore && cpairs == 0 && !tune.cols_lsu && !tune.no_pipe &&
-        (kind == LK_C2C || (kind == LK_R2C && AFFT_PIPE_R2C) || kind == LK_C2R) && get_cols_pipe(logl, kind, &kp) &&
-        kp.kind == op.k.kind && kp.logl == op.k.logl && !op.k.tc)
+    if (AFFT_COLS_PIPE && !f64 && !tc && cols && cpairs == 0 && !tune.cols_lsu && !tune.no_pipe && !op.k.tc &&
+        (tstore ? kind == LK_C2C && get_cols_pipe_tstore(logl, &kp)
+                : (kind == LK_C2C || (kind == LK_R2C && AFFT_PIPE_R2C) || kind == LK_C2R) &&
+                      get_cols_pipe(logl, kind, &kp)) &&
+        kp.kind == op.k.kind && kp.logl == op.k.logl && kp.tstore == op.k.tstore)
       op.k = kp;
     // another tile width for 256- and 512-point complex cols passes, when tuned so
     LineKernel ka;
@@ -1144,7 +1146,7 @@ int Plan::launch(const float* src_re, const float* src_im, float* dst_re, float*
       // costs more, 2048² c2r 0.0324 vs 0.0300 ms)
       const long long slots = (long long)sm_count * op.k.pipe_ctas;
       if (op.k.pipe && sm_count > 0 && (op.k.logl == 11 || op.grid >= 2 * slots) && tma_tile(p, op.k, &tm) &&
-          (!(AFFT_PIPE_BULK_STORE && op.k.kind == LK_C2C) || tma_tile_out(p, op.k, &tmo))) {
+          (!(AFFT_PIPE_BULK_STORE && op.k.kind == LK_C2C && !op.k.tstore) || tma_tile_out(p, op.k, &tmo))) {
         // persistent: at most pipe_ctas CTAs per SM, each walking tiles gridDim.x apart
         const long long g = std::min<long long>(op.grid, slots);
         op.k.pipe<<<(unsigned)g, op.threads, op.k.pipe_smem, st>>>(p, tm, tmo, op.grid);

@@ -118,3 +118,4 @@ def test_pipe_1024_c2r(dev, dims, batch):
     for j in range(batch):
         ref = O.oracle64("ri", dims, a[j * h:(j + 1) * h], b[j * h:(j + 1) * h])
         assert O.rel_l2(got[j * n:(j + 1) * n], ref) <= TOL, (dims, batch, j)
+
