@@ -84,8 +84,9 @@ bool get_cols_tma_tstore(int logl, LineKernel* out);
 // loads of the interleaved tile (k_cols_tma_pairs.cu)
 bool get_cols_tma_pairs(int logl, bool tstore, int pairs, LineKernel* out);
 
-// 2048-point cols passes {C2C, R2C (unsplit), C2R} over split planes in the
-// persistent TMA-pipelined form (k_cols_pipe.cu): out->pipe set, out->tma and
+// 2048-point cols passes {C2C, C2R, and R2C unsplit when AFFT_PIPE_R2C} and
+// 1024-point {C2C, C2R} over split planes in the persistent TMA-pipelined
+// form (k_cols_pipe.cu): out->pipe (and out->grouped_pipe) set, out->tma and
 // out->fn the one-tile-per-CTA kernels of the same shape
 bool get_cols_pipe(int logl, int kind, LineKernel* out);
 // the 1024-point four-step pass A (transposing store, split planes) in that form
@@ -213,7 +214,8 @@ LineKernel make_plane_kernel() {
   return k;
 }
 
-// a 2048-point cols pass with its pipelined form (AFFT_PIPE_C lines per tile)
+// a 1024- or 2048-point cols pass with its pipelined form (8 lines per tile;
+// AFFT_PIPE_C at 2048 points)
 template <int LOGL, int KIND, bool TSTORE = false>
 LineKernel make_pipe_kernel() {
   constexpr int C = LOGL == 11 ? AFFT_PIPE_C : 8;

@@ -1,19 +1,21 @@
-// Persistent, TMA-pipelined cols passes of 2048 points (line_fft_pipe).
+// Persistent, TMA-pipelined cols passes of 2048 and 1024 points
+// (line_fft_pipe, and line_fft_pipe_grouped for the multi-transform queue).
 //
 // A 2048-point cols tile of 8 lines is 128 KB, so the one-tile-per-CTA
 // kernels (line_fft, line_fft_tma) fit one CTA per SM.  Each SM then loads
 // a tile, runs its stages and stores it in sequence, and HBM idles while the
-// SMs compute.  Here one CTA per SM walks the tiles blockIdx.x,
-// blockIdx.x + gridDim.x, ...  As soon as its threads have taken tile i out
+// SMs compute.  Here one CTA per SM (two for 1024-point tiles) walks the
+// tiles blockIdx.x, blockIdx.x + gridDim.x, ...  As soon as its threads have taken tile i out
 // of the raw buffer (into registers), one thread issues the TMA loads of the
 // CTA's next tile into that buffer.  Those land while tile i's stages run and
 // its results are stored (the C2C pass: by TMA from the exchange buffer, one
 // plane at a time).
 //
 // Shared memory: the raw tile ([re: L rows x C][im: L rows x C] floats,
-// 128 KB, as tma_load_tile lays it out) and a separate exchange buffer through
+// 128 KB at 2048 points, as tma_load_tile lays it out) and a separate exchange buffer through
 // which the stages pass the re parts first, then the im parts.  Element j of
-// line c sits at float (j + j/8) * C + c there (one pad row per 8: 72 KB).  A
+// line c sits at float (j + j/8) * C + c there (one pad row per 8: 72 KB;
+// 1024-point tiles pad one row per 4, below).  A
 // warp covers 4 consecutive threads t (lanes 8 apart share a line), so each
 // access touches 4 rows, and the padding puts them on 4 different 8-bank
 // groups for the radix-8 scatter (rows 8 apart), the radix-16 scatter

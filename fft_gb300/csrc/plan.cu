@@ -385,13 +385,14 @@ static View inter_view(int b, long long off = 0) {  // re,im pairs in one array
 #ifndef AFFT_TMA_C2R11
 #define AFFT_TMA_C2R11 1
 #endif
-// 2048-point cols passes over split planes: the persistent TMA-pipelined
-// kernels (one CTA per SM loading its next tile under the current one's stages)
+// 1024- and 2048-point cols passes over split planes: the persistent
+// TMA-pipelined kernels (one or two CTAs per SM, each loading its next tile
+// under the current one's stages)
 #ifndef AFFT_COLS_PIPE
 #define AFFT_COLS_PIPE 1
 #endif
 // the last two axes of complex N-D transforms in one plane-fused pass
-// (plane_fft) where a plane of 2^12 .. 2^14 points fits one CTA
+// (plane_fft) where a plane of 2^8 .. 2^14 points fits one CTA
 #ifndef AFFT_PLANE
 #define AFFT_PLANE 1
 #endif
@@ -498,7 +499,7 @@ struct Builder {
           kt.tstore == op.k.tstore && !op.k.tc)
         op.k = kt;
     }
-    // 2048-point cols passes: the persistent pipelined form (the R2C pass
+    // 1024- and 2048-point cols passes: the persistent pipelined form (the R2C pass
     // unsplit); at launch the one-tile-per-CTA kernels of the same shape run
     // where the bound arrays miss the TMA rules
     LineKernel kp;

@@ -108,7 +108,7 @@ struct Tuning {
   int cols_c = 0;     // lines per CTA of the 256- and 512-point complex cols passes (0: the default)
   int passes = 0;     // 1D complex axes of 2^20 points and more: 0 the built-in rule (three passes
                       // from 2^21), 2 two passes, 3 three passes
-  int no_pipe = 0;    // 1: 2048-point cols passes keep their one-tile-per-CTA kernels
+  int no_pipe = 0;    // 1: 1024- and 2048-point cols passes keep their one-tile-per-CTA kernels
   int no_plane = 0;   // the last two axes of complex N-D transforms where a plane-fused pass applies:
                       // 0 the built-in rule, 1 a pass each, 2 the plane pass at any plane count
 };
