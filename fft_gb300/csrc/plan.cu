@@ -499,9 +499,11 @@ struct Builder {
           kt.tstore == op.k.tstore && !op.k.tc)
         op.k = kt;
     }
-    // 1024- and 2048-point cols passes: the persistent pipelined form (the R2C pass
-    // unsplit); at launch the one-tile-per-CTA kernels of the same shape run
-    // where the bound arrays miss the TMA rules
+    // 1024- and 2048-point cols passes: the persistent pipelined form (C2C
+    // and C2R; the unsplit R2C and the transposing store only in their opt-in
+    // builds); at launch the one-tile-per-CTA kernels of the same shape run
+    // where the bound arrays miss the TMA rules or, at 1024 points, the tiles
+    // are too few
     LineKernel kp;
     if (AFFT_COLS_PIPE && !f64 && !tc && cols && cpairs == 0 && !tune.cols_lsu && !tune.no_pipe && !op.k.tc &&
         (tstore ? kind == LK_C2C && get_cols_pipe_tstore(logl, &kp)
