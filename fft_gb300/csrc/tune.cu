@@ -7,7 +7,9 @@
 //    pass takes);
 //  - for long 1D real inverses, the real pre-pass riding in the first
 //    four-step pass (over mirrored column pairs) or standalone;
-//  - cols passes loading their input tiles by TMA or through the LSU;
+//  - cols passes loading their input tiles by TMA or through the LSU, and the
+//    1024- and 2048-point ones in the persistent pipelined form or one tile per
+//    CTA;
 //  - the tile width (lines per CTA) of 256- and 512-point complex cols passes;
 //  - the plain FP32 form or the split-precision tensor-core form of the
 //    passes that have one;
@@ -83,9 +85,9 @@ std::string key_of(int kind, int ndim, const long long* dims, long long batch, i
 
 // file format: a JSON object, one entry per line:
 //   "<key>": {"split": S, "real_inv": R, "cols_lsu": U, "tc": T, "cols_c": C, "passes": P,
-//             "no_plane": N, "ms": M},
-// (entries of the older forms, without no_plane, passes or cols_lsu / tc /
-// cols_c, still load)
+//             "no_plane": N, "no_pipe": Q, "ms": M},
+// (entries of the older forms, without no_pipe, no_plane, passes or cols_lsu /
+// tc / cols_c, still load)
 void load_locked(TuneCache& C) {
   if (C.loaded) return;
   C.loaded = true;
@@ -102,6 +104,11 @@ void load_locked(TuneCache& C) {
     if (!b) continue;
     Entry e;
     if (std::sscanf(b + 1,
+                    " : {\"split\": %d, \"real_inv\": %d, \"cols_lsu\": %d, \"tc\": %d, \"cols_c\": %d, "
+                    "\"passes\": %d, \"no_plane\": %d, \"no_pipe\": %d, \"ms\": %lf",
+                    &e.t.split, &e.t.real_inv, &e.t.cols_lsu, &e.t.tc, &e.t.cols_c, &e.t.passes, &e.t.no_plane,
+                    &e.t.no_pipe, &e.ms) == 9 ||
+        std::sscanf(b + 1,
                     " : {\"split\": %d, \"real_inv\": %d, \"cols_lsu\": %d, \"tc\": %d, \"cols_c\": %d, "
                     "\"passes\": %d, \"no_plane\": %d, \"ms\": %lf",
                     &e.t.split, &e.t.real_inv, &e.t.cols_lsu, &e.t.tc, &e.t.cols_c, &e.t.passes, &e.t.no_plane,
@@ -131,8 +138,9 @@ void save_locked(const TuneCache& C) {
     const Tuning& t = kv.second.t;
     std::fprintf(f,
                  "\"%s\": {\"split\": %d, \"real_inv\": %d, \"cols_lsu\": %d, \"tc\": %d, \"cols_c\": %d, "
-                 "\"passes\": %d, \"no_plane\": %d, \"ms\": %.6f}%s\n",
-                 kv.first.c_str(), t.split, t.real_inv, t.cols_lsu, t.tc, t.cols_c, t.passes, t.no_plane, kv.second.ms,
+                 "\"passes\": %d, \"no_plane\": %d, \"no_pipe\": %d, \"ms\": %.6f}%s\n",
+                 kv.first.c_str(), t.split, t.real_inv, t.cols_lsu, t.tc, t.cols_c, t.passes, t.no_plane, t.no_pipe,
+                 kv.second.ms,
                  ++i < C.table.size() ? "," : "");
   }
   std::fprintf(f, "}\n");
@@ -213,7 +221,8 @@ int tune_shape(int kind, int ndim, const long long* dims, long long batch, int f
       for (int lsu = 0; lsu < 2; lsu++)
         for (int tc = 0; tc < 2; tc++)
           for (int w : widths)
-          for (int np = 0; np < nplane; np++) {
+          for (int np = 0; np < nplane; np++)
+          for (int npipe = 0; npipe < 2; npipe++) {
             Tuning t;
             t.split = split;
             t.real_inv = real_inv;
@@ -222,6 +231,7 @@ int tune_shape(int kind, int ndim, const long long* dims, long long batch, int f
             t.cols_c = w;
             t.passes = pass_forms[pf];
             t.no_plane = np;
+            t.no_pipe = npipe;
             auto P = build_plan(kind, ndim, dims, batch, format, false, 0, &t);
             if (!P) {
               clear_error();
@@ -273,16 +283,16 @@ int tune_shape(int kind, int ndim, const long long* dims, long long batch, int f
       const Tuning& t = cands[i].first;
       snprintf(buf, sizeof buf,
                "%s{\"split\":%d,\"real_inv\":%d,\"cols_lsu\":%d,\"tc\":%d,\"cols_c\":%d,\"passes\":%d,"
-               "\"no_plane\":%d,\"launches\":%zu,\"ms\":%.6f}",
-               i ? "," : "", t.split, t.real_inv, t.cols_lsu, t.tc, t.cols_c, t.passes, t.no_plane,
+               "\"no_plane\":%d,\"no_pipe\":%d,\"launches\":%zu,\"ms\":%.6f}",
+               i ? "," : "", t.split, t.real_inv, t.cols_lsu, t.tc, t.cols_c, t.passes, t.no_plane, t.no_pipe,
                cands[i].second->ops.size(), times[i]);
       *report += buf;
     }
     const Tuning& t = out->t;
     snprintf(buf, sizeof buf,
              "],\"chosen\":{\"split\":%d,\"real_inv\":%d,\"cols_lsu\":%d,\"tc\":%d,\"cols_c\":%d,\"passes\":%d,"
-             "\"no_plane\":%d,\"ms\":%.6f}}",
-             t.split, t.real_inv, t.cols_lsu, t.tc, t.cols_c, t.passes, t.no_plane, out->ms);
+             "\"no_plane\":%d,\"no_pipe\":%d,\"ms\":%.6f}}",
+             t.split, t.real_inv, t.cols_lsu, t.tc, t.cols_c, t.passes, t.no_plane, t.no_pipe, out->ms);
     *report += buf;
   }
   return 0;

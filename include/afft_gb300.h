@@ -230,7 +230,8 @@ AFFT_GB300_API size_t afft_gb300_plan_describe(int kind, size_t ndim,
  * (device, kind, dims, batch, format).  The variants: the four-step split
  * of axes longer than one CTA holds (which half the first pass takes); for
  * long 1D real inverses, the real pre-pass fused into the first pass or run
- * on its own; cols passes loading their tiles by TMA or through the LSU;
+ * on its own; cols passes loading their tiles by TMA or through the LSU, and
+ * the 1024- and 2048-point ones pipelined or one tile per CTA;
  * 8, 16 or 32 lines per CTA for 256- and 512-point complex cols passes; the
  * plain FP32 or the split-precision tensor-core form of the passes that have
  * one; 1D complex axes of 2^20 to 2^22 points in two passes or three; and the

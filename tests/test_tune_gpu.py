@@ -95,6 +95,19 @@ def test_tune_weighs_large_planes_at_small_counts(dev):
     batched_parity("c", [8, 128, 128], 2)
 
 
+def test_tune_weighs_pipelined_form(dev):
+    # 2048-point cols passes: the persistent pipelined kernel or one tile
+    # per CTA (at 2048 points the one-tile complex pass loads through the
+    # LSU, so that variant and cols_lsu build the same launches); both timed,
+    # the faster kept
+    rep = G.tune("c", [2048, 2048], 4)
+    cands = rep["candidates"]
+    assert {c["no_pipe"] for c in cands} == {0, 1}, rep
+    timed = [c for c in cands if c["ms"] > 0]
+    assert rep["chosen"]["ms"] == min(c["ms"] for c in timed)
+    batched_parity("c", [2048, 2048], 4)
+
+
 def test_tune_shape_without_choices(dev):
     rep = G.tune("c", [1024], 64)
     assert len(rep["candidates"]) == 1 and rep["chosen"]["ms"] < 0
