@@ -3,13 +3,18 @@
 // real inverse (the paired C2R pass) writing its output so, L = 2^7 .. 2^9
 #include "kernels.h"
 
+// lines per CTA of the 512-point paired R2C pass (16: the cols default)
+#ifndef AFFT_PAIRED_C9
+#define AFFT_PAIRED_C9 16
+#endif
+
 namespace agb {
 
 bool get_r2c_paired_pairs(int logl, LineKernel* out) {
   switch (logl) {
     case 7: *out = make_line_kernel<7, true, LK_R2C_PAIRED, false, false, 1>(); return true;
     case 8: *out = make_line_kernel<8, true, LK_R2C_PAIRED, false, false, 1>(); return true;
-    case 9: *out = make_line_kernel<9, true, LK_R2C_PAIRED, false, false, 1>(); return true;
+    case 9: *out = make_line_kernel<9, true, LK_R2C_PAIRED, false, false, 1, AFFT_PAIRED_C9>(); return true;
     case 10: *out = make_line_kernel<10, true, LK_R2C_PAIRED, false, false, 1>(); return true;
     case 11: *out = make_line_kernel<11, true, LK_R2C_PAIRED, false, false, 1>(); return true;
     default: return false;
