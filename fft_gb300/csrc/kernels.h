@@ -11,6 +11,7 @@ typedef void (*LineKernelFn)(LineParams);
 typedef void (*GroupedKernelFn)(const Segment*, const int*, long long);
 typedef void (*LineKernelTmaFn)(LineParams, TmaTile);
 typedef void (*LineKernelPipeFn)(LineParams, TmaTile, TmaTile, long long);
+typedef void (*LineKernelPairedFn)(LineParams, PairedTma);
 
 struct LineKernel {
   LineKernelFn fn;
@@ -35,6 +36,9 @@ struct LineKernel {
   size_t pipe_smem = 0;              // its dynamic shared memory (raw tile + exchange buffer)
   int pipe_ctas = 1;                 // its resident CTAs per SM (the grid is at most that many per SM)
   GroupedKernelFn grouped_pipe = nullptr;   // its queue form (segments with tensor maps), or null
+  LineKernelPairedFn paired_tma = nullptr;  // the paired R2C pass over input pairs with TMA-loaded tiles
+                                            // (line_fft_paired_tma), or null
+  size_t paired_smem = 0;                   // its dynamic shared memory
   int plane_log1 = 0;                // plane kernels (plane_fft): log2 of the rows per plane (the column
                                      // axis); logl is then log2 of the row length; 0 for line kernels
 };
@@ -55,7 +59,8 @@ bool get_cols_c2c_pairs(int logl, bool tstore, int pairs, LineKernel* out);
 // the transposing-store half of it (k_cols_pairs_ts.cu)
 bool get_cols_c2c_pairs_tstore(int logl, int pairs, LineKernel* out);
 // the paired R2C pass (four-step pass B of a long 1D real forward) with its
-// input as float2 pairs, lines of 2^7 .. 2^11 points
+// input as float2 pairs, lines of 2^7 .. 2^11 points; at 2^9 and 2^10 points
+// with the TMA-fed form (paired_tma) too
 bool get_r2c_paired_pairs(int logl, LineKernel* out);
 // the paired C2R pass (four-step pass A of a long 1D real inverse) with its
 // output as float2 pairs, lines of 2^7 .. 2^9 points
@@ -187,6 +192,17 @@ LineKernel make_tma_kernel() {
   LineKernel k = make_line_kernel<LOGL, true, KIND, TSTORE, false, UNIT, C>();
   k.tma = &line_fft_tma<LOGL, C, KIND, TSTORE, UNIT>;
   k.grouped_tma = &line_fft_grouped<LOGL, C, true, KIND, TSTORE, false, UNIT, true>;
+  return k;
+}
+
+// the paired R2C pass over input pairs, with its TMA-fed form
+template <int LOGL>
+LineKernel make_paired_tma_kernel() {
+  LineKernel k = make_line_kernel<LOGL, true, LK_R2C_PAIRED, false, false, 1>();
+  constexpr int C = lines_per_cta_k<LOGL, true, LK_R2C_PAIRED>(), H = C / 2, L2 = 1 << LOGL;
+  k.paired_tma = &line_fft_paired_tma<LOGL, C>;
+  const size_t raw = (size_t)L2 * (2 * H + 2 * H + 4 + 4) * sizeof(float);
+  k.paired_smem = raw > k.smem ? raw : k.smem;   // the raw tile aliases the exchange buffer
   return k;
 }
 

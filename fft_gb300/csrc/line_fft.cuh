@@ -495,7 +495,11 @@ __device__ __forceinline__ long long paired_column(int c, long long a, long long
 // (k = k1 + L1 k2, written where the unfused pass B would write Z[k]), and
 // the column-0 thread of k2 = 0 also writes X[L] (element L2 of line
 // (o, 0)).  Lines come in whole tiles: L1 is a multiple of C.
-template <int LOGL, int C, bool PIN = false>
+// TMA: the tile is already in shared memory as line_fft_paired_tma lays it
+// out: the aligned half [L2 rows][2H floats] (columns a .. a+H-1), the
+// mirrored half from the 16-byte boundary below it [L2 rows][2H + 4 floats]
+// (columns L1-a-H .. L1-a+1), and in tile 0 column L1/2 [L2 rows][4 floats].
+template <int LOGL, int C, bool PIN = false, bool TMA = false>
 __device__ __forceinline__ void r2c_paired_body(const LineParams& p, long long cta) {
   using Sc = Sched<LOGL>;
   constexpr int L2 = Sc::L, E = Sc::E, T = Sc::T, H = C / 2;
@@ -512,7 +516,18 @@ __device__ __forceinline__ void r2c_paired_body(const LineParams& p, long long c
   const long long q = o * L1 + k1;
 
   float2 v[E];
-  {
+  if constexpr (TMA) {
+    static_assert(PIN, "TMA tiles: the paired pass over input pairs");
+    const float* raw = reinterpret_cast<const float*>(smem_raw);
+    const float* mi = raw + L2 * 2 * H;
+    const float* src = c < H ? raw + 2 * c
+                       : (a == 0 && c == H) ? mi + L2 * (2 * H + 4)
+                                            : mi + 2 * (H - (c - H));   // column L1 - a - m at H - m
+    const int pitch = c < H ? 2 * H : (a == 0 && c == H) ? 4 : 2 * H + 4;
+#pragma unroll
+    for (int e = 0; e < E; e++) v[e] = *reinterpret_cast<const float2*>(src + (t + T * e) * pitch);
+    __syncthreads();   // the tile is read before the stages reuse the buffer
+  } else {
     const long long base = line_off(p.in, q);
     const long long S = (long long)T * p.in.es;
     const float* pr = p.in.re + base + (long long)t * p.in.es;
@@ -1505,6 +1520,47 @@ line_fft_tma(const LineParams p, const __grid_constant__ TmaTile tm) {
   extern __shared__ __align__(1024) float2 smem_raw[];
   if (!tma_load_tile<C>(p, tm, blockIdx.x, &mbar, smem_raw)) return;
   line_fft_body<LOGL, C, true, KIND, TSTORE, false, UNIT, true>(p, blockIdx.x);
+}
+
+// The paired R2C pass (four-step pass B of a long 1D real forward, input
+// pairs) with its tile loaded by TMA.  Its mirrored half starts 8 bytes off a
+// 16-byte boundary, so it comes as a box of H + 2 pair-columns from the
+// boundary below (tile 0's box runs past the last column and reads the fill
+// value there), the aligned half as a box of H, and tile 0's column L1/2 as a
+// box of 2 (16 bytes).  Maps over the pairs array as {2 L1 floats, L2 rows,
+// transforms}.
+struct PairedTma {
+  CUtensorMap al, mi, sp;   // boxes of 2H, 2H + 4 and 4 floats x box_rows rows
+  int box_rows;
+};
+
+template <int LOGL, int C>
+__global__ void __launch_bounds__(Sched<LOGL>::T * C, min_ctas<Sched<LOGL>::T * C>())
+line_fft_paired_tma(const LineParams p, const __grid_constant__ PairedTma pt) {
+  constexpr int L2 = Sched<LOGL>::L, H = C / 2;
+  __shared__ __align__(8) uint64_t mbar;
+  extern __shared__ __align__(1024) float2 smem_raw[];
+  const long long L1 = p.pcols, tiles = L1 / C, cta = blockIdx.x;
+  const long long o = cta / tiles, a = (cta % tiles) * H;
+  const uint32_t mb = smem_u32(&mbar);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    const uint32_t bytes = (uint32_t)L2 * (2 * H + 2 * H + 4 + (a == 0 ? 4 : 0)) * 4u;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(bytes) : "memory");
+    const uint32_t d = smem_u32(smem_raw);
+    const uint32_t mi = (uint32_t)L2 * 2 * H * 4u, sp = mi + (uint32_t)L2 * (2 * H + 4) * 4u;
+    const int z = (int)o;
+    for (int r = 0; r < L2; r += pt.box_rows) {
+      tma_load_3d(d + (uint32_t)r * 2 * H * 4u, &pt.al, (int)(2 * a), r, z, mb);
+      tma_load_3d(d + mi + (uint32_t)r * (2 * H + 4) * 4u, &pt.mi, (int)(2 * (L1 - a - H)), r, z, mb);
+      if (a == 0) tma_load_3d(d + sp + (uint32_t)r * 16u, &pt.sp, (int)L1, r, z, mb);
+    }
+  }
+  __syncthreads();   // the barrier's set-up is visible before anyone waits on it
+  if (!tma_wait_tile(mb, p.err)) return;
+  r2c_paired_body<LOGL, C, true, true>(p, cta);
 }
 
 // One launch of a multi-transform queue: a device-side table of segments

@@ -538,7 +538,14 @@ struct Builder {
         fail("kernel shared memory configuration failed");
         return;
       }
-      if (op.k.tma) {
+      if (op.k.paired_tma && op.k.paired_smem > 48 * 1024 &&
+          cudaFuncSetAttribute((const void*)op.k.paired_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)op.k.paired_smem) != cudaSuccess) {
+        cudaGetLastError();
+        fail("kernel shared memory configuration failed");
+        return;
+      }
+      if (op.k.tma || op.k.paired_tma) {
         op.p.err = tc_error_word();
         if (!op.p.err) {
           fail("error word allocation failed");
@@ -1112,6 +1119,38 @@ bool tma_tile_out(const LineParams& p, const LineKernel& k, TmaTile* tm) {
   return encode_tile(p.out, p.nlines, 1LL << k.logl, k.lines_per_cta, false, tm);
 }
 
+// The paired R2C pass's maps (line_fft_paired_tma): its input is one
+// interleaved array of pairs, lines (o, k1) the columns of L1 = pcols per
+// transform, rows at element stride es, transforms hi apart; whole
+// transforms, 16-byte aligned base and strides.
+bool tma_paired(const LineParams& p, const LineKernel& k, PairedTma* pt) {
+  const LineIO& in = p.in;
+  const long long L2 = 1LL << k.logl, C = k.lines_per_cta, H = C / 2, L1 = p.pcols;
+  if (in.im != in.re + 1 || in.lo != 2 || L1 <= 0 || (1LL << in.qshift) != L1 || in.qmask != L1 - 1 || L1 % C ||
+      p.nlines % L1 || (reinterpret_cast<uintptr_t>(in.re) & 15))
+    return false;
+  const long long nouter = p.nlines / L1;
+  const long long rs = in.es * 4, bs = nouter > 1 ? in.hi * 4 : L2 * in.es * 4;
+  if (rs % 16 || bs % 16 || rs <= 0 || bs <= 0 || rs >= (1LL << 40) || bs >= (1LL << 40)) return false;
+  auto encode = tensor_map_encoder();
+  if (!encode) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)(2 * L1), (cuuint64_t)L2, (cuuint64_t)nouter};
+  const cuuint64_t strides[2] = {(cuuint64_t)rs, (cuuint64_t)bs};
+  const int br = (int)std::min<long long>(L2, 256);
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const cuuint32_t widths[3] = {(cuuint32_t)(2 * H), (cuuint32_t)(2 * H + 4), 4};
+  CUtensorMap* maps[3] = {&pt->al, &pt->mi, &pt->sp};
+  for (int i = 0; i < 3; i++) {
+    const cuuint32_t box[3] = {widths[i], (cuuint32_t)br, 1};
+    if (encode(maps[i], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)in.re, dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return false;
+  }
+  pt->box_rows = br;
+  return true;
+}
+
 bool op_tables_ok(const Op& op) {
   if (op.type != OP_LINE) return op.type != OP_REAL || op.rp.rtw;
   return op.p.tw && (op.k.kind == LK_C2C || op.p.rtw) &&
@@ -1144,11 +1183,14 @@ int Plan::launch(const float* src_re, const float* src_im, float* dst_re, float*
       p.in = bind(op.in, base, esz);
       p.out = bind(op.out, base, esz);
       TmaTile tm, tmo{};
+      PairedTma pt;
       // (1024-point tiles take the pipelined kernel from two per CTA slot:
       // with one each it has nothing to prefetch and its float exchange
       // costs more, 2048² c2r 0.0324 vs 0.0300 ms)
       const long long slots = (long long)sm_count * op.k.pipe_ctas;
-      if (op.k.pipe && sm_count > 0 && (op.k.logl == 11 || op.grid >= 2 * slots) && tma_tile(p, op.k, &tm) &&
+      if (op.k.paired_tma && tma_paired(p, op.k, &pt)) {
+        op.k.paired_tma<<<(unsigned)op.grid, op.threads, op.k.paired_smem, st>>>(p, pt);
+      } else if (op.k.pipe && sm_count > 0 && (op.k.logl == 11 || op.grid >= 2 * slots) && tma_tile(p, op.k, &tm) &&
           (!(AFFT_PIPE_BULK_STORE && op.k.kind == LK_C2C && !op.k.tstore) || tma_tile_out(p, op.k, &tmo))) {
         // persistent: at most pipe_ctas CTAs per SM, each walking tiles gridDim.x apart
         const long long g = std::min<long long>(op.grid, slots);

@@ -133,6 +133,8 @@ int* tc_error_word();
 // The tensor maps of a cols pass's TMA-fed kernel for the bound arrays, or
 // false when they do not meet its alignment rules (launch k.fn instead).
 bool tma_tile(const LineParams& p, const LineKernel& k, TmaTile* tm);
+// the paired R2C pass's three maps over its input pairs, when the arrays allow them
+bool tma_paired(const LineParams& p, const LineKernel& k, PairedTma* pt);
 
 // Whether every table an op's kernel reads is present (device plans).
 bool op_tables_ok(const Op& op);
