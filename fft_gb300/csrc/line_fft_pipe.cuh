@@ -65,10 +65,14 @@
 
 namespace agb {
 
-// the passes that store by TMA
-template <int KIND>
+#ifndef AFFT_PIPE_BULK10
+#define AFFT_PIPE_BULK10 1
+#endif
+// the passes that store by TMA (the complex ones; at 1024 points when
+// AFFT_PIPE_BULK10)
+template <int LOGL, int KIND>
 constexpr bool pipe_bulk() {
-  return AFFT_PIPE_BULK_STORE && KIND == LK_C2C;
+  return AFFT_PIPE_BULK_STORE && KIND == LK_C2C && (LOGL == 11 || AFFT_PIPE_BULK10);
 }
 
 // Rows of the exchange buffer.  2048-point schedule (radix 8, 16, 16; T =
@@ -437,7 +441,7 @@ line_fft_pipe(const __grid_constant__ LineParams p, const __grid_constant__ TmaT
   extern __shared__ __align__(1024) float2 smem_raw[];
   float* raw = reinterpret_cast<float*>(smem_raw);
   const uint32_t mb = smem_u32(&mbar), raw_s = smem_u32(raw);
-  pipe_loop<LOGL, C, KIND, pipe_bulk<KIND>() && !TSTORE, TSTORE>(
+  pipe_loop<LOGL, C, KIND, pipe_bulk<LOGL, KIND>() && !TSTORE, TSTORE>(
       blockIdx.x, ntiles, mb, raw, raw + 2 * Sched<LOGL>::L * C, &tmo,
       [&](long long tile, long long* cta) -> const LineParams& {
         *cta = tile;
