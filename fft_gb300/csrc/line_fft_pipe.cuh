@@ -68,11 +68,17 @@ namespace agb {
 #ifndef AFFT_PIPE_BULK10
 #define AFFT_PIPE_BULK10 1
 #endif
+#ifndef AFFT_PIPE_BULK_C2R10
+#define AFFT_PIPE_BULK_C2R10 1
+#endif
 // the passes that store by TMA (the complex ones; at 1024 points when
-// AFFT_PIPE_BULK10)
+// AFFT_PIPE_BULK10; the 1024-point C2R pass when AFFT_PIPE_BULK_C2R10:
+// 3.5-5.5% faster there, where at 2048 points the C2R pass measured 1-2.5%
+// slower with them)
 template <int LOGL, int KIND>
 constexpr bool pipe_bulk() {
-  return AFFT_PIPE_BULK_STORE && KIND == LK_C2C && (LOGL == 11 || AFFT_PIPE_BULK10);
+  return AFFT_PIPE_BULK_STORE && ((KIND == LK_C2C && (LOGL == 11 || AFFT_PIPE_BULK10)) ||
+                                  (KIND == LK_C2R && LOGL == 10 && AFFT_PIPE_BULK_C2R10));
 }
 
 // Rows of the exchange buffer.  2048-point schedule (radix 8, 16, 16; T =
@@ -221,7 +227,7 @@ __device__ __forceinline__ void pipe_loop(long long first, long long ntiles, uin
   static_assert(((LOGL == 11 && (C == 8 || C == 4) && Sc::radix(0) == 8) || (LOGL == 10 && C == 8 && Sc::radix(0) == 4)) &&
                     E == 16,
                 "the exchange rows are those of 8- or 4-line 2048-point and 8-line 1024-point tiles");
-  static_assert(!BULK || KIND == LK_C2C, "TMA stores: the complex pass");
+  static_assert(!BULK || KIND == LK_C2C || KIND == LK_C2R, "TMA stores: the complex and C2R passes");
   static_assert(!TSTORE || (KIND == LK_C2C && LOGL == 10 && C == 8 && !BULK),
                 "the transposing store: 8-line 1024-point complex tiles");
   const int tid = threadIdx.x;

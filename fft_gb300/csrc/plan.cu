@@ -1191,7 +1191,9 @@ int Plan::launch(const float* src_re, const float* src_im, float* dst_re, float*
       if (op.k.paired_tma && tma_paired(p, op.k, &pt)) {
         op.k.paired_tma<<<(unsigned)op.grid, op.threads, op.k.paired_smem, st>>>(p, pt);
       } else if (op.k.pipe && sm_count > 0 && (op.k.logl == 11 || op.grid >= 2 * slots) && tma_tile(p, op.k, &tm) &&
-          (!(AFFT_PIPE_BULK_STORE && op.k.kind == LK_C2C && !op.k.tstore && (op.k.logl == 11 || AFFT_PIPE_BULK10)) ||
+          (!(AFFT_PIPE_BULK_STORE && !op.k.tstore &&
+             ((op.k.kind == LK_C2C && (op.k.logl == 11 || AFFT_PIPE_BULK10)) ||
+              (op.k.kind == LK_C2R && op.k.logl == 10 && AFFT_PIPE_BULK_C2R10))) ||
            tma_tile_out(p, op.k, &tmo))) {
         // persistent: at most pipe_ctas CTAs per SM, each walking tiles gridDim.x apart
         const long long g = std::min<long long>(op.grid, slots);
