@@ -12,6 +12,7 @@ typedef void (*GroupedKernelFn)(const Segment*, const int*, long long);
 typedef void (*LineKernelTmaFn)(LineParams, TmaTile);
 typedef void (*LineKernelPipeFn)(LineParams, TmaTile, TmaTile, long long);
 typedef void (*LineKernelPairedFn)(LineParams, PairedTma);
+typedef void (*LineKernelTmaBulkFn)(LineParams, TmaTile, TmaTile);
 
 struct LineKernel {
   LineKernelFn fn;
@@ -31,6 +32,8 @@ struct LineKernel {
   LineKernelTmaFn tma; // the same pass with its input tile loaded by TMA (cols passes over
                        // split planes), or null
   GroupedKernelFn grouped_tma;   // its grouped form (queue segments with tensor maps), or null
+  LineKernelTmaBulkFn tma_bulk = nullptr;   // the TMA-fed form that also stores by TMA
+                                            // (line_fft_tma_bulk), or null
   LineKernelPipeFn pipe = nullptr;   // the persistent TMA-pipelined form (line_fft_pipe), or null;
                                      // launched on at most one CTA per SM with the tile count
   size_t pipe_smem = 0;              // its dynamic shared memory (raw tile + exchange buffer)
@@ -192,6 +195,8 @@ LineKernel make_tma_kernel() {
   LineKernel k = make_line_kernel<LOGL, true, KIND, TSTORE, false, UNIT, C>();
   k.tma = &line_fft_tma<LOGL, C, KIND, TSTORE, UNIT>;
   k.grouped_tma = &line_fft_grouped<LOGL, C, true, KIND, TSTORE, false, UNIT, true>;
+  if constexpr (KIND == LK_C2C && !TSTORE && UNIT == 0 && ((LOGL == 9 && AFFT_TMA_BULK9) || (LOGL == 8 && AFFT_TMA_BULK8)))
+    k.tma_bulk = &line_fft_tma_bulk<LOGL, C>;
   return k;
 }
 

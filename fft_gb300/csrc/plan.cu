@@ -516,7 +516,7 @@ struct Builder {
     if (tune.cols_c && !f64 && !tc && cols && !tstore && !cpairs && kind == LK_C2C &&
         get_cols_c2c_alt(logl, tune.cols_c, &ka)) {
       op.k = ka;
-      if (!AFFT_COLS_TMA || tune.cols_lsu) op.k.tma = nullptr, op.k.grouped_tma = nullptr;
+      if (!AFFT_COLS_TMA || tune.cols_lsu) op.k.tma = nullptr, op.k.grouped_tma = nullptr, op.k.tma_bulk = nullptr;
     }
     op.in = in;
     op.out = out;
@@ -532,6 +532,9 @@ struct Builder {
                                 (int)op.k.smem) != cudaSuccess ||
            (op.k.tma && cudaFuncSetAttribute((const void*)op.k.tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)op.k.smem) != cudaSuccess) ||
+           (op.k.tma_bulk && cudaFuncSetAttribute((const void*)op.k.tma_bulk,
+                                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                  (int)op.k.smem) != cudaSuccess) ||
            (op.k.pipe && cudaFuncSetAttribute((const void*)op.k.pipe, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               (int)op.k.pipe_smem) != cudaSuccess))) {
         cudaGetLastError();
@@ -1198,6 +1201,8 @@ int Plan::launch(const float* src_re, const float* src_im, float* dst_re, float*
         // persistent: at most pipe_ctas CTAs per SM, each walking tiles gridDim.x apart
         const long long g = std::min<long long>(op.grid, slots);
         op.k.pipe<<<(unsigned)g, op.threads, op.k.pipe_smem, st>>>(p, tm, tmo, op.grid);
+      } else if (op.k.tma_bulk && tma_tile(p, op.k, &tm) && tma_tile_out(p, op.k, &tmo)) {
+        op.k.tma_bulk<<<(unsigned)op.grid, op.threads, op.smem, st>>>(p, tm, tmo);
       } else if (op.k.tma && tma_tile(p, op.k, &tm)) {
         op.k.tma<<<(unsigned)op.grid, op.threads, op.smem, st>>>(p, tm);
       } else {

@@ -4,6 +4,8 @@ against the FP64 oracle:
 tile counts below, at and above one per SM and not multiples of the grid,
 in place and out of place, the four-step twiddle, and arrays off a 16-byte
 boundary, where the one-tile-per-CTA kernels of the same shape run instead.
+Also the one-tile 512-point complex cols pass that stores its tile by TMA
+(line_fft_tma_bulk).
 Tolerance: relative L2 <= 2e-6, as the other parity tests."""
 import numpy as np
 import pytest
@@ -119,3 +121,21 @@ def test_pipe_1024_c2r(dev, dims, batch):
         ref = O.oracle64("ri", dims, a[j * h:(j + 1) * h], b[j * h:(j + 1) * h])
         assert O.rel_l2(got[j * n:(j + 1) * n], ref) <= TOL, (dims, batch, j)
 
+
+# 512-point complex cols passes: TMA loads and TMA stores, one tile of 8
+# columns per CTA (1 tile, 153 tiles, 64 tiles per transform, a 3D middle
+# axis, the strided axis of a 2^18-point four-step with its twiddle)
+@pytest.mark.parametrize("dims,batch", [([512, 8], 1), ([512, 8], 153), ([512, 512], 8), ([4, 512, 64], 3),
+                                        ([64, 512, 256], 2), ([1 << 18], 4)], ids=str)
+@pytest.mark.parametrize("kind", ["c", "ci"])
+def test_tma_store_512(dev, kind, dims, batch):
+    for inplace in (False, True):
+        err = _c2c(kind, dims, batch, dev, inplace=inplace, seed=batch)
+        assert err <= TOL, (kind, dims, batch, inplace, err)
+
+
+@pytest.mark.parametrize("pad", [1, 2])
+def test_tma_store_512_unaligned(dev, pad):
+    # off a 16-byte boundary neither map encodes and the LSU kernel runs
+    for dims, batch in (([512, 64], 2), ([512, 512], 1)):
+        assert _c2c("c", dims, batch, dev, pad=pad, seed=pad) <= TOL, (dims, pad)
