@@ -195,8 +195,10 @@ LineKernel make_tma_kernel() {
   LineKernel k = make_line_kernel<LOGL, true, KIND, TSTORE, false, UNIT, C>();
   k.tma = &line_fft_tma<LOGL, C, KIND, TSTORE, UNIT>;
   k.grouped_tma = &line_fft_grouped<LOGL, C, true, KIND, TSTORE, false, UNIT, true>;
-  if constexpr (KIND == LK_C2C && !TSTORE && UNIT == 0 && ((LOGL == 9 && AFFT_TMA_BULK9) || (LOGL == 8 && AFFT_TMA_BULK8)))
-    k.tma_bulk = &line_fft_tma_bulk<LOGL, C>;
+  if constexpr (!TSTORE && UNIT == 0 &&
+                ((KIND == LK_C2C && ((LOGL == 9 && AFFT_TMA_BULK9) || (LOGL == 8 && AFFT_TMA_BULK8))) ||
+                 (KIND == LK_C2R && ((LOGL == 9 && AFFT_TMA_BULK_C2R9) || (LOGL == 8 && AFFT_TMA_BULK_C2R8)))))
+    k.tma_bulk = &line_fft_tma_bulk<LOGL, C, KIND>;
   return k;
 }
 

@@ -913,15 +913,33 @@ __device__ __forceinline__ void rows_stage_out_reals(const LineParams& p, long l
 // TMA: the CTA's input tile is already in the exchange buffer, put there by
 // tma_load_tile (cols mode, split planes): [re: L rows x C][im: L rows x C]
 // floats; C2R tiles hold bins 0 .. L-1 there and read bin L directly.
-// BULK: a C2C cols pass over a TMA-loaded tile leaves its output planes in
-// the tile's buffer ([L][C] floats each, re then im) for the caller to store
-// by TMA (line_fft_tma_bulk) instead of storing them itself.
+// The output planes of a cols tile (element t + T e of line c in v[e]) into
+// the tile's buffer st, [L][C] floats each, re then im, for TMA stores: a
+// half-warp writes 16 adjacent columns of one row (no bank conflicts).  The
+// first barrier waits for the stages' last reads of the buffer; the proxy
+// fence makes the writes visible to the TMA unit.
+template <int L, int C, int T, int E>
+__device__ __forceinline__ void bulk_stage_out(const float2 (&v)[E], int t, int c, float* st) {
+  __syncthreads();
+#pragma unroll
+  for (int e = 0; e < E; e++) {
+    st[(t + T * e) * C + c] = v[e].x;
+    st[L * C + (t + T * e) * C + c] = v[e].y;
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  __syncthreads();
+}
+
+// BULK: a C2C or C2R cols pass over a TMA-loaded tile leaves its output
+// planes in the tile's buffer (bulk_stage_out) for the caller to store by TMA
+// (line_fft_tma_bulk) instead of storing them itself.
 template <int LOGL, int C, bool COLS, int KIND, bool TSTORE, bool TC = false, int UNIT = 0, bool TMA = false,
           bool BULK = false>
 __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta, TcState* ts = nullptr) {
   static_assert(!TMA || (COLS && !TC && (UNIT == 0 || KIND == LK_C2C) && (!TSTORE || KIND == LK_C2C)),
                 "TMA tiles: cols passes");
-  static_assert(!BULK || (TMA && KIND == LK_C2C && !TSTORE && UNIT == 0), "TMA stores: split C2C cols tiles");
+  static_assert(!BULK || (TMA && (KIND == LK_C2C || KIND == LK_C2R) && !TSTORE && UNIT == 0),
+                "TMA stores: split C2C and C2R cols tiles");
   if constexpr (KIND == LK_R2C_HALF) {
     static_assert(COLS && !TSTORE && !TC, "the split R2C pass is a plain cols pass");
     r2c_half_body<LOGL, C>(p, cta);
@@ -1201,16 +1219,7 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
         for (int e = 0; e < E; e++) v[e] = cswap(v[e]);
       }
       if constexpr (BULK) {
-        // (a half-warp writes 16 adjacent columns of one row: no bank conflicts)
-        float* st = reinterpret_cast<float*>(smem_raw);
-        __syncthreads();   // the stages' last reads of the buffer are done
-#pragma unroll
-        for (int e = 0; e < E; e++) {
-          st[(t + T * e) * C + c] = v[e].x;
-          st[L * C + (t + T * e) * C + c] = v[e].y;
-        }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // visible to the TMA unit
-        __syncthreads();
+        bulk_stage_out<L, C, T>(v, t, c, reinterpret_cast<float*>(smem_raw));
         return;
       }
       bool staged_out = false;
@@ -1270,6 +1279,10 @@ __device__ __forceinline__ void line_fft_body(const LineParams& p, long long cta
   } else if constexpr (KIND == LK_C2R) {
 #pragma unroll
     for (int e = 0; e < E; e++) v[e] = cswap(v[e]);
+    if constexpr (BULK) {
+      bulk_stage_out<L, C, T>(v, t, c, reinterpret_cast<float*>(smem_raw));
+      return;
+    }
     bool staged_out = false;
     if constexpr (!COLS && T <= AFFT_C2R_OUT_T && E == 16 && !TC) {
       if (reals_contiguous(p.out, L)) {

@@ -73,6 +73,15 @@
 #ifndef AFFT_TMA_BULK8
 #define AFFT_TMA_BULK8 0
 #endif
+// the same for the 512- and 256-point C2R cols passes: 512 x 64 x 64 x 16
+// c2r 0.1113 vs 0.1133 ms at 256 points (on); 1024² x 16 c2r 0.0703 vs
+// 0.0683 ms at 512 points (slower, off)
+#ifndef AFFT_TMA_BULK_C2R9
+#define AFFT_TMA_BULK_C2R9 0
+#endif
+#ifndef AFFT_TMA_BULK_C2R8
+#define AFFT_TMA_BULK_C2R8 1
+#endif
 
 namespace agb {
 
@@ -495,11 +504,11 @@ line_fft_pipe_grouped(const Segment* __restrict__ segs, const int* __restrict__ 
       });
 }
 
-// A one-tile C2C cols pass (as line_fft_tma) whose output planes go back out
-// by TMA from the tile's buffer (output maps tmo; whole tiles, the host's
-// tma_tile rules for the output).  Thread 0 waits until the stores have read
-// the buffer before the CTA ends.
-template <int LOGL, int C>
+// A one-tile C2C or C2R cols pass (as line_fft_tma) whose output planes go
+// back out by TMA from the tile's buffer (output maps tmo; whole tiles, the
+// host's tma_tile rules for the output).  Thread 0 waits until the stores
+// have read the buffer before the CTA ends.
+template <int LOGL, int C, int KIND>
 __global__ void __launch_bounds__(Sched<LOGL>::T * C, min_ctas<Sched<LOGL>::T * C>())
 line_fft_tma_bulk(const __grid_constant__ LineParams p, const __grid_constant__ TmaTile tm,
                   const __grid_constant__ TmaTile tmo) {
@@ -507,7 +516,7 @@ line_fft_tma_bulk(const __grid_constant__ LineParams p, const __grid_constant__ 
   __shared__ __align__(8) uint64_t mbar;
   extern __shared__ __align__(1024) float2 smem_raw[];
   if (!tma_load_tile<C>(p, tm, blockIdx.x, &mbar, smem_raw)) return;
-  line_fft_body<LOGL, C, true, LK_C2C, false, false, 0, true, true>(p, blockIdx.x);
+  line_fft_body<LOGL, C, true, KIND, false, false, 0, true, true>(p, blockIdx.x);
   if (threadIdx.x == 0) {
     const uint32_t s = smem_u32(smem_raw);
     pipe_store_plane<L, C>(p, &tmo.re, tmo.box_rows, blockIdx.x, s);

@@ -4,8 +4,8 @@ against the FP64 oracle:
 tile counts below, at and above one per SM and not multiples of the grid,
 in place and out of place, the four-step twiddle, and arrays off a 16-byte
 boundary, where the one-tile-per-CTA kernels of the same shape run instead.
-Also the one-tile 512-point complex cols pass that stores its tile by TMA
-(line_fft_tma_bulk).
+Also the one-tile 512-point complex and 256-point C2R cols passes that
+store their tile by TMA (line_fft_tma_bulk).
 Tolerance: relative L2 <= 2e-6, as the other parity tests."""
 import numpy as np
 import pytest
@@ -139,3 +139,33 @@ def test_tma_store_512_unaligned(dev, pad):
     # off a 16-byte boundary neither map encodes and the LSU kernel runs
     for dims, batch in (([512, 64], 2), ([512, 512], 1)):
         assert _c2c("c", dims, batch, dev, pad=pad, seed=pad) <= TOL, (dims, pad)
+
+
+def _c2r(dims, batch, dev, pad=0, seed=0):
+    n = int(np.prod(dims))
+    h = O.half_elems(dims)
+    rng = np.random.default_rng(seed)
+    a = rng.standard_normal(h * batch).astype(np.float32)
+    b = rng.standard_normal(h * batch).astype(np.float32)
+    from test_plane_gpu import _dev
+    d = _dev(np.zeros(n * batch, np.float32), dev, pad)
+    G.BatchPlan("ri", dims, batch).launch(_dev(a, dev, pad), _dev(b, dev, pad), d, None)
+    torch.cuda.synchronize()
+    got = d.cpu().numpy()
+    return max(O.rel_l2(got[j * n:(j + 1) * n], O.oracle64("ri", dims, a[j * h:(j + 1) * h], b[j * h:(j + 1) * h]))
+               for j in range(batch))
+
+
+# 256-point C2R cols passes (real inverse along a 512-point axis): TMA loads
+# and stores, 16 columns per tile (one tile per transform, 153 tiles, 3D),
+# and off a 16-byte boundary the load-only or LSU kernels
+@pytest.mark.parametrize("dims,batch", [([512, 16], 3), ([512, 16], 153), ([512, 512], 4), ([512, 8, 64], 3),
+                                        ([512, 64, 64], 2)], ids=str)
+def test_tma_store_256_c2r(dev, dims, batch):
+    assert _c2r(dims, batch, dev, seed=batch) <= TOL, (dims, batch)
+
+
+@pytest.mark.parametrize("pad", [1, 2])
+def test_tma_store_256_c2r_unaligned(dev, pad):
+    for dims, batch in (([512, 64], 2), ([512, 512], 1)):
+        assert _c2r(dims, batch, dev, pad=pad, seed=pad) <= TOL, (dims, pad)
