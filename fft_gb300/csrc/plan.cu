@@ -1007,11 +1007,11 @@ std::string describe_plan(const Plan& P) {
     if (op.type == OP_LINE) {
       snprintf(buf, sizeof buf,
                "{\"type\":\"line\",\"logl\":%d,\"cols\":%d,\"lk\":%d,\"tstore\":%d,\"tc\":%d,\"C\":%d,"
-               "\"halves\":%d,\"unit\":%d,\"tma\":%d,\"pipe\":%d,\"plane\":%d,"
+               "\"halves\":%d,\"unit\":%d,\"tma\":%d,\"tma_store\":%d,\"pipe\":%d,\"plane\":%d,"
                "\"threads\":%d,\"smem\":%zu,\"grid\":%lld,\"nlines\":%lld,\"inverse\":%d,"
                "\"tw_n\":%lld,\"tw_qmask\":%lld,\"tw_qshift\":%d,\"real_L\":%lld,\"pcols\":%lld,",
                op.k.logl, op.k.cols, op.k.kind, op.k.tstore, op.k.tc, op.k.lines_per_cta, op.k.halves, op.k.unit,
-               op.k.tma != nullptr, op.k.pipe != nullptr, op.k.plane_log1, op.threads,
+               op.k.tma != nullptr, op.k.tma_bulk != nullptr, op.k.pipe != nullptr, op.k.plane_log1, op.threads,
                op.smem,
                op.grid, op.p.nlines, op.p.inverse, op.p.tw_n, op.p.tw_qmask, op.p.tw_qshift, op.real_L, op.p.pcols);
     } else if (op.type == OP_REAL) {

@@ -129,6 +129,7 @@ def test_pipe_1024_c2r(dev, dims, batch):
                                         ([64, 512, 256], 2), ([1 << 18], 4)], ids=str)
 @pytest.mark.parametrize("kind", ["c", "ci"])
 def test_tma_store_512(dev, kind, dims, batch):
+    assert sum(op.get("tma_store", 0) for op in describe(kind, dims, batch)["ops"]) == 1
     for inplace in (False, True):
         err = _c2c(kind, dims, batch, dev, inplace=inplace, seed=batch)
         assert err <= TOL, (kind, dims, batch, inplace, err)
@@ -162,6 +163,7 @@ def _c2r(dims, batch, dev, pad=0, seed=0):
 @pytest.mark.parametrize("dims,batch", [([512, 16], 3), ([512, 16], 153), ([512, 512], 4), ([512, 8, 64], 3),
                                         ([512, 64, 64], 2)], ids=str)
 def test_tma_store_256_c2r(dev, dims, batch):
+    assert sum(op.get("tma_store", 0) for op in describe("ri", dims, batch)["ops"]) == 1
     assert _c2r(dims, batch, dev, seed=batch) <= TOL, (dims, batch)
 
 

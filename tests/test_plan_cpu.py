@@ -217,3 +217,23 @@ def test_tma_fed_passes(kind, dims, batch, expect):
     d = describe(kind, dims, batch)
     got = [(op.get("tma", 0), op.get("pipe", 0)) for op in d["ops"] if op["type"] == "line"]
     assert got == expect, (got, d["ops"])
+
+
+@pytest.mark.parametrize("kind,dims,batch,expect", [
+    ("c", [512, 512], 64, [0, 1]),             # 512-point complex cols pass: TMA stores
+    ("ci", [8, 512, 64], 2, [0, 1, 0]),        # the 512-point middle axis; the 8-point one has no TMA form
+    ("c", [1 << 18], 4, [0, 1]),               # 512 x 512 four-step: pass B (pass A: the transposing store,
+                                               # TMA loads only)
+    ("c", [256, 256, 256], 1, [0, 0, 0]),      # 256-point complex cols passes: per-thread stores (measured)
+    ("ri", [512, 512], 64, [0, 1]),            # 256-point C2R cols pass: TMA stores
+    ("ri", [1024, 1024], 16, [0, 0]),          # 512-point C2R cols pass: per-thread stores (measured)
+    ("r", [512, 512], 64, [0, 0]),             # R2C cols passes: per-thread stores
+    ("c", [2048, 2048], 2, [0, 0]),            # the pipelined passes store by TMA on their own
+], ids=str)
+def test_tma_store_passes(kind, dims, batch, expect):
+    """Which passes have the one-tile TMA kernel that also stores its tile by
+    TMA (line_fft_tma_bulk), taken at launch when both the input and the
+    output maps encode."""
+    d = describe(kind, dims, batch)
+    got = [op.get("tma_store", 0) for op in d["ops"] if op["type"] == "line"]
+    assert got == expect, (got, d["ops"])
