@@ -8,8 +8,8 @@
 // tiles blockIdx.x, blockIdx.x + gridDim.x, ...  As soon as its threads have taken tile i out
 // of the raw buffer (into registers), one thread issues the TMA loads of the
 // CTA's next tile into that buffer.  Those land while tile i's stages run and
-// its results are stored (the C2C pass: by TMA from the exchange buffer, one
-// plane at a time).
+// its results are stored (the C2C passes and the 1024-point C2R pass: by TMA
+// from the exchange buffer, one plane at a time).
 //
 // Shared memory: the raw tile ([re: L rows x C][im: L rows x C] floats,
 // 128 KB at 2048 points, as tma_load_tile lays it out) and a separate exchange buffer through
@@ -33,7 +33,8 @@
 // their own: 1% faster for C2R, and for C2C with BULK_STORE.  BULK_STORE: the
 // C2C pass stages each output plane in the exchange buffer and stores it with
 // TMA (cp.async.bulk.tensor) instead of per-thread stores: 1-3% faster for
-// C2C, 1-2.5% slower for C2R (which keeps per-thread stores).
+// C2C, 1-2.5% slower for the 2048-point C2R pass (which keeps per-thread
+// stores; the 1024-point one below gains from them).
 #ifndef AFFT_PIPE_LATE_ISSUE
 #define AFFT_PIPE_LATE_ISSUE 1
 #endif
@@ -237,7 +238,7 @@ __device__ __forceinline__ void pipe_store_plane(const LineParams& p, const CUte
 // the post-pass through the exchange buffer), LK_C2R (the pre-pass from the
 // raw tile, bin L read directly).  Split planes in, split planes out; every
 // tile whole (the host's tma_tile rules).  BULK: the output planes go out by
-// TMA (the output maps tmo; C2C only).
+// TMA (the output maps tmo; C2C and C2R).
 template <int LOGL, int C, int KIND, bool BULK, bool TSTORE, class Prep, class Issue>
 __device__ __forceinline__ void pipe_loop(long long first, long long ntiles, uint32_t mb, float* raw, float* xs,
                                           const TmaTile* tmo, const Prep& prep, const Issue& issue) {

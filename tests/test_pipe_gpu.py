@@ -1,5 +1,6 @@
 """GPU parity of the persistent TMA-pipelined 1024- and 2048-point cols
-passes (line_fft_pipe: C2C, with TMA output stores at 2048 points, and C2R)
+passes (line_fft_pipe: C2C, and C2R; TMA output stores for C2C and the
+1024-point C2R pass)
 against the FP64 oracle:
 tile counts below, at and above one per SM and not multiples of the grid,
 in place and out of place, the four-step twiddle, and arrays off a 16-byte
