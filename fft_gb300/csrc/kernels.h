@@ -196,8 +196,10 @@ LineKernel make_tma_kernel() {
   k.tma = &line_fft_tma<LOGL, C, KIND, TSTORE, UNIT>;
   k.grouped_tma = &line_fft_grouped<LOGL, C, true, KIND, TSTORE, false, UNIT, true>;
   if constexpr (!TSTORE && UNIT == 0 &&
-                ((KIND == LK_C2C && ((LOGL == 9 && AFFT_TMA_BULK9) || (LOGL == 8 && AFFT_TMA_BULK8))) ||
-                 (KIND == LK_C2R && ((LOGL == 9 && AFFT_TMA_BULK_C2R9) || (LOGL == 8 && AFFT_TMA_BULK_C2R8)))))
+                ((KIND == LK_C2C &&
+                  ((LOGL == 10 && AFFT_TMA_BULK10) || (LOGL == 9 && AFFT_TMA_BULK9) || (LOGL == 8 && AFFT_TMA_BULK8))) ||
+                 (KIND == LK_C2R && ((LOGL == 10 && AFFT_TMA_BULK_C2R10) || (LOGL == 9 && AFFT_TMA_BULK_C2R9) ||
+                                     (LOGL == 8 && AFFT_TMA_BULK_C2R8)))))
     k.tma_bulk = &line_fft_tma_bulk<LOGL, C, KIND>;
   return k;
 }

@@ -83,6 +83,15 @@
 #ifndef AFFT_TMA_BULK_C2R8
 #define AFFT_TMA_BULK_C2R8 1
 #endif
+// the one-tile 1024-point complex and C2R kernels (taken where the tiles are
+// too few for the pipelined ones): 1024² x 2 c2c 0.0272 vs 0.0293-0.0304
+// ms, 1024 x 512 x 4 ci 0.0272 vs 0.0293 ms (on); C2R level (off)
+#ifndef AFFT_TMA_BULK10
+#define AFFT_TMA_BULK10 1
+#endif
+#ifndef AFFT_TMA_BULK_C2R10
+#define AFFT_TMA_BULK_C2R10 0
+#endif
 
 namespace agb {
 

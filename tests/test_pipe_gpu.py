@@ -5,8 +5,8 @@ against the FP64 oracle:
 tile counts below, at and above one per SM and not multiples of the grid,
 in place and out of place, the four-step twiddle, and arrays off a 16-byte
 boundary, where the one-tile-per-CTA kernels of the same shape run instead.
-Also the one-tile 512-point complex and 256-point C2R cols passes that
-store their tile by TMA (line_fft_tma_bulk).
+Also the one-tile 1024- and 512-point complex and 256-point C2R cols
+passes that store their tile by TMA (line_fft_tma_bulk).
 Tolerance: relative L2 <= 2e-6, as the other parity tests."""
 import numpy as np
 import pytest
@@ -172,3 +172,16 @@ def test_tma_store_256_c2r(dev, dims, batch):
 def test_tma_store_256_c2r_unaligned(dev, pad):
     for dims, batch in (([512, 64], 2), ([512, 512], 1)):
         assert _c2r(dims, batch, dev, pad=pad, seed=pad) <= TOL, (dims, pad)
+
+
+# 1024-point complex cols passes below the pipelined kernel's threshold
+# (fewer than 608 tiles): the one-tile kernel with TMA loads and stores
+# (1 tile, 128, 256 and 512 tiles, the four-step's pass B with its twiddle)
+@pytest.mark.parametrize("dims,batch", [([1024, 8], 1), ([1024, 1024], 1), ([1024, 512], 4), ([1024, 1024], 4),
+                                        ([1 << 20], 2)], ids=str)
+@pytest.mark.parametrize("kind", ["c", "ci"])
+def test_tma_store_1024_one_tile(dev, kind, dims, batch):
+    assert sum(op.get("tma_store", 0) for op in describe(kind, dims, batch)["ops"]) == 1
+    for inplace in (False, True):
+        err = _c2c(kind, dims, batch, dev, inplace=inplace, seed=batch)
+        assert err <= TOL, (kind, dims, batch, inplace, err)

@@ -229,11 +229,15 @@ def test_tma_fed_passes(kind, dims, batch, expect):
     ("ri", [1024, 1024], 16, [0, 0]),          # 512-point C2R cols pass: per-thread stores (measured)
     ("r", [512, 512], 64, [0, 0]),             # R2C cols passes: per-thread stores
     ("c", [2048, 2048], 2, [0, 0]),            # the pipelined passes store by TMA on their own
+    ("c", [1024, 1024], 2, [0, 1]),            # 1024 points: the one-tile form below the pipelined
+                                               # kernel's tile threshold stores by TMA too
+    ("ri", [2048, 2048], 1, [0, 0]),           # 1024-point C2R one-tile form: per-thread stores (measured)
 ], ids=str)
 def test_tma_store_passes(kind, dims, batch, expect):
     """Which passes have the one-tile TMA kernel that also stores its tile by
     TMA (line_fft_tma_bulk), taken at launch when both the input and the
-    output maps encode."""
+    output maps encode (and, for 1024-point passes, when the tiles are too
+    few for the pipelined kernel)."""
     d = describe(kind, dims, batch)
     got = [op.get("tma_store", 0) for op in d["ops"] if op["type"] == "line"]
     assert got == expect, (got, d["ops"])
